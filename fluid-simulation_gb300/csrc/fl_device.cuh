@@ -1,0 +1,175 @@
+// fl_device.cuh — device-side layout and helpers of the FLIP/PIC substep.
+//
+// Arithmetic follows the reference's WGSL shaders expression by expression,
+// written with explicit round-to-nearest intrinsics (__fadd_rn, __fmul_rn, ...)
+// so that nvcc cannot contract a*b+c into an FMA: the f32 path then produces the
+// same bits as the reference arithmetic evaluated op by op.
+// SH/ below = app/crates/fluid-lab/src/gpu/shaders/ of the reference project.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fl {
+
+constexpr uint8_t CELL_SOLID = 0, CELL_LIQUID = 1, CELL_AIR = 2;
+constexpr int CHUNK = 256;        // cells per reduction chunk (the 256-wide workgroup of cg_reduce.wgsl)
+constexpr int CG_GROUPS = 4;      // 256-thread chunk groups per CG block
+constexpr int CG_THREADS = CHUNK * CG_GROUPS;
+constexpr int SCAN_ITEMS = 4;     // counts per thread in the bin scan
+constexpr int SCAN_THREADS = 1024;
+constexpr int SCAN_TILE = SCAN_ITEMS * SCAN_THREADS;
+constexpr int BIG_BUCKET_SMEM = 4096;  // larger buckets use the global-memory rank pass
+constexpr int TILE = 8;           // P2G tile edge (cells)
+
+// Device copy of the step settings.  Derived scalars are computed once on the
+// host with the same f32 operations the shaders use (see fl_host.cpp).
+struct DevParams {
+    uint32_t nx, ny, nz, C;
+    uint32_t F3[3], n;
+    float h, inv_h, dt, fixed_scale;
+    float rho, flip, friction, maxs;     // maxs = max(cfl,1)*h/dt (g2p.wgsl:159-160)
+    float origin[3], scale_rhs;          // rho*h*h/dt (cg_init.wgsl:68)
+    float grav[3], coeff_grad;           // (dt/rho)/h (gradient.wgsl:65)
+    float rest, stiff, drift_clamp, tol_sq;  // spc; clamp(tol,0,0.1)^2 in f32
+    float lo[3], half_dt;                // origin + h*1.05 (g2p.wgsl:166)
+    float hi[3], pad0;                   // origin + extent - h*1.05 (g2p.wgsl:167)
+    uint32_t thresh, dilation, warm, iters;
+    uint32_t precision, advect_order, nchunks, pad1;
+    double tol_sq_d;
+};
+
+// Per-step device counters and results.
+struct DevStats {
+    // zeroed at the start of every substep (first 32 bytes)
+    uint32_t liquid;
+    uint32_t strays;
+    uint32_t big_buckets;
+    uint32_t cg_iters;
+    uint32_t barrier;     // CG grid-barrier arrival counter
+    uint32_t pad0[3];
+    // kept until the host reads it
+    uint32_t status;      // 0 or an fl_status code recorded by a kernel
+    uint32_t pad1[3];
+    double rs_init, rs_final;
+};
+constexpr size_t DEVSTATS_STEP_BYTES = 32;
+
+// All device buffers of one handle.  Particles are 2 float4 per particle
+// (pos.xyzw, vel.xyzw) exactly like the reference buffer (fluid.rs:116-123).
+struct DevBufs {
+    const DevParams* prm;
+    DevStats* st;
+    float4* part_in;       // particles at step start (read by binning, written by G2P)
+    float4* part_sorted;   // bin-ordered copy; pos.w = 1 marks a stray particle
+    float4* part_out;      // G2P destination (== part_in for the handle path)
+    uint32_t* ids_in;      // may be null
+    uint32_t* ids_sorted;
+    uint32_t* keys;
+    uint32_t* perm;
+    uint32_t* scratch_u32; // capacity-sized scratch (big-bucket rank pass)
+    uint32_t* stray_list;
+    uint32_t* counts;
+    uint32_t* offsets;
+    uint32_t* cursor;
+    uint32_t* spine;
+    uint32_t* big_list;
+    uint8_t* ct;
+    uint8_t* chunk_flag;
+    int32_t* num[3];
+    int32_t* den[3];
+    float* vel[3];
+    float* sav[3];
+    float *p, *r, *dA, *dB, *q;
+    float* part_rr;        // per-chunk f32 tree partials
+    float* part_dq;
+    double* chunk_rr64;    // per-chunk f64 partials of the initial residual
+    double* cta_part64;    // [2][max CTAs] f64 partials (FL_CG_F64)
+};
+
+// ---------------------------------------------------------------------------
+// helpers (device code only; fl_host.cpp sees the layout above)
+#if defined(__CUDACC__)
+
+__device__ __forceinline__ uint32_t face_dim(const DevParams& P, int axis, int b) {
+    uint32_t n = b == 0 ? P.nx : (b == 1 ? P.ny : P.nz);
+    return n + (axis == b ? 1u : 0u);
+}
+
+// mark.wgsl:39-43: clamp(floor((p - o)/h), 0, n-1).  fmaxf returns the other
+// operand for NaN, so a NaN coordinate lands in cell 0.
+__device__ __forceinline__ uint32_t key_coord(float pos, float origin, float h, uint32_t n) {
+    float g = __fdiv_rn(__fsub_rn(pos, origin), h);
+    float f = floorf(g);
+    float c = fminf(fmaxf(f, 0.0f), (float)(n - 1u));
+    return (uint32_t)c;
+}
+
+__device__ __forceinline__ uint32_t cell_key(const DevParams& P, float4 pos, uint32_t* kc) {
+    kc[0] = key_coord(pos.x, P.origin[0], P.h, P.nx);
+    kc[1] = key_coord(pos.y, P.origin[1], P.h, P.ny);
+    kc[2] = key_coord(pos.z, P.origin[2], P.h, P.nz);
+    return kc[0] + P.nx * (kc[1] + P.ny * kc[2]);
+}
+
+// True when the multiply-form cell coordinate (p-o)*inv_h of scatter.wgsl:94
+// disagrees with the division-form bin on some axis (an ulp tie or a clamped
+// bin).  Such particles are scattered by the separate stray pass.
+__device__ __forceinline__ bool is_stray(const DevParams& P, float4 pos, const uint32_t* kc) {
+    float q0 = __fmul_rn(__fsub_rn(pos.x, P.origin[0]), P.inv_h);
+    float q1 = __fmul_rn(__fsub_rn(pos.y, P.origin[1]), P.inv_h);
+    float q2 = __fmul_rn(__fsub_rn(pos.z, P.origin[2]), P.inv_h);
+    return floorf(q0) != (float)kc[0] || floorf(q1) != (float)kc[1] || floorf(q2) != (float)kc[2];
+}
+
+__device__ __forceinline__ int32_t floor_to_i32(float x) { return __float2int_rz(floorf(x)); }
+
+// SH/scatter.wgsl:71-72: i32(round(x)) — round half to even, saturating.
+__device__ __forceinline__ int32_t fixed_round(float x) { return __float2int_rn(x); }
+
+// The reference's weight ordering w = wx * wy * wz with the loop order
+// dk (outer), dj, di (inner) of scatter.wgsl:55-67.
+__device__ __forceinline__ float tent(float t, int d) { return d == 1 ? t : __fsub_rn(1.0f, t); }
+
+// Grid barrier over all blocks of a cooperative launch.  Arrival is a
+// release-add on a counter that only grows within one launch; waiting is an
+// acquire-load spin bounded by %globaltimer (about 2 s).  On expiry, or when
+// another block has recorded an error, it records FL_TIMEOUT and returns false.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_release_add(uint32_t* p, uint32_t v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+#endif  // __CUDACC__
+}  // namespace fl
+
+// Launchers (defined in the .cu files); all enqueue on `s` and return the
+// launch error.
+namespace fl {
+struct LaunchCfg {
+    int num_sms;
+    int cg_blocks;         // cooperative grid size for the CG kernel
+    int particle_blocks;   // grid-stride particle kernels
+};
+cudaError_t launch_bin(const DevBufs& b, const LaunchCfg& L, uint32_t C, uint32_t cap, cudaStream_t s);
+cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s);
+cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz,
+                       cudaStream_t s);
+cudaError_t launch_grid_prep(const DevBufs& b, uint32_t C, cudaStream_t s);
+cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
+cudaError_t launch_project(const DevBufs& b, uint32_t C, cudaStream_t s);
+cudaError_t launch_g2p(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
+cudaError_t launch_impulse(float4* part, const DevParams* prm, float dx, float dy, float dz,
+                           const LaunchCfg& L, cudaStream_t s);
+int cg_max_blocks_per_sm();
+// Stand-alone CG on prepared cell arrays (used by fl_solve_pressure).
+cudaError_t launch_solve_init(const DevBufs& b, uint32_t C, const float* div, cudaStream_t s);
+}  // namespace fl

@@ -1,0 +1,454 @@
+// fl_grid.cu — cell classification, P2G, grid preparation and projection.
+//
+//   k_classify   classify.wgsl:25-61 (Solid/Liquid/Air, dilation, liquid count)
+//   k_p2g_tile   scatter.wgsl:44-117 in gather form: one block owns a tile of
+//                faces and accumulates the fixed-point terms of every particle
+//                in the tile and a one-cell halo (read from the sorted bins) in
+//                shared memory; each face is written once, no global atomics
+//   k_p2g_strays the same terms for particles flagged as strays (their
+//                multiply-form cell differs from their bin), by global atomics
+//   k_grid_prep  normalize.wgsl + save_vel.wgsl + forces.wgsl + boundaries.wgsl
+//                per face, then divergence.wgsl + cg_init.wgsl + the first
+//                cg_reduce.wgsl tree per 256-cell chunk
+//   k_project    gradient.wgsl (the following boundaries pass is a no-op: faces
+//                touching a solid are already zero and gradient skips them)
+#include "fl_device.cuh"
+
+namespace fl {
+
+__global__ void __launch_bounds__(256) k_classify(DevBufs b, uint32_t C) {
+    const DevParams& P = *b.prm;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    bool liquid = false;
+    if (c < C) {
+        const uint32_t nx = P.nx, ny = P.ny, nz = P.nz;
+        const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+        const bool boundary = i == 0 || j == 0 || k == 0 || i == nx - 1 || j == ny - 1 || k == nz - 1;
+        uint8_t t = CELL_SOLID;
+        if (!boundary) {
+            const uint32_t th = P.thresh;
+            const uint32_t* occ = b.counts;
+            liquid = occ[c] >= th;
+            if (!liquid && P.dilation) {
+                liquid = occ[c - 1] >= th || occ[c + 1] >= th || occ[c - nx] >= th || occ[c + nx] >= th ||
+                         occ[c - nx * ny] >= th || occ[c + nx * ny] >= th;
+            }
+            t = liquid ? CELL_LIQUID : CELL_AIR;
+        }
+        b.ct[c] = t;
+    }
+    const uint32_t m = __ballot_sync(0xffffffffu, liquid);
+    if ((threadIdx.x & 31u) == 0 && m) atomicAdd(&b.st->liquid, (uint32_t)__popc(m));
+}
+
+// ---------------------------------------------------------------------------
+// P2G
+
+struct TileGeom {
+    int x0, y0, z0;     // first cell of the tile
+    int xe, ye, ze;     // one past the last cell of the tile
+    int n[3];           // grid cells per axis
+};
+
+// Face range owned along axis b by the tile, for faces of `axis`.
+__device__ __forceinline__ void owned_range(const TileGeom& T, int axis, int b, int& lo, int& hi) {
+    const int s = b == 0 ? T.x0 : (b == 1 ? T.y0 : T.z0);
+    const int e = b == 0 ? T.xe : (b == 1 ? T.ye : T.ze);
+    lo = s;
+    hi = (axis == b && e == T.n[b]) ? e + 1 : e;
+}
+
+constexpr int TS_U = (TILE + 1) * TILE * TILE;  // shared slots per axis
+
+__device__ __forceinline__ void p2g_component(const DevParams& P, const TileGeom& T, int axis, const float q[3],
+                                              float vcomp, int32_t* s_num, int32_t* s_den) {
+    float g[3], t[3];
+    int base[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+        g[b] = __fadd_rn(q[b], b == axis ? 0.0f : -0.5f);
+        base[b] = floor_to_i32(g[b]);
+        t[b] = __fsub_rn(g[b], (float)base[b]);
+    }
+    int lo[3], hi[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) owned_range(T, axis, b, lo[b], hi[b]);
+    const int sx = TILE + (axis == 0), sy = TILE + (axis == 1);
+    const float scale = P.fixed_scale;
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        const int kk = base[2] + dk;
+        if (kk < lo[2] || kk >= hi[2]) continue;
+        const float wz = tent(t[2], dk);
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            const int jj = base[1] + dj;
+            if (jj < lo[1] || jj >= hi[1]) continue;
+            const float wy = tent(t[1], dj);
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const int ii = base[0] + di;
+                if (ii < lo[0] || ii >= hi[0]) continue;
+                const float wx = tent(t[0], di);
+                const float w = __fmul_rn(__fmul_rn(wx, wy), wz);
+                if (w <= 0.0f) continue;
+                const int li = (ii - T.x0) + sx * ((jj - T.y0) + sy * (kk - T.z0));
+                atomicAdd(&s_num[li], fixed_round(__fmul_rn(__fmul_rn(w, vcomp), scale)));
+                atomicAdd(&s_den[li], fixed_round(__fmul_rn(w, scale)));
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_p2g_tile(DevBufs b, int tiles_x, int tiles_y) {
+    __shared__ int32_t s_num[3][TS_U];
+    __shared__ int32_t s_den[3][TS_U];
+    const DevParams& P = *b.prm;
+    const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
+    const int tid = blockIdx.x;
+    const int tx = tid % tiles_x, ty = (tid / tiles_x) % tiles_y, tz = tid / (tiles_x * tiles_y);
+    TileGeom T;
+    T.x0 = tx * TILE; T.y0 = ty * TILE; T.z0 = tz * TILE;
+    T.xe = min(T.x0 + TILE, nx); T.ye = min(T.y0 + TILE, ny); T.ze = min(T.z0 + TILE, nz);
+    T.n[0] = nx; T.n[1] = ny; T.n[2] = nz;
+    for (int i = threadIdx.x; i < 3 * TS_U; i += blockDim.x) {
+        (&s_num[0][0])[i] = 0;
+        (&s_den[0][0])[i] = 0;
+    }
+    __syncthreads();
+
+    // Halo of one cell: every non-stray particle whose taps reach an owned face
+    // has its bin in [x0-1, xe] x [y0-1, ye] x [z0-1, ze] (clamped to the grid).
+    const int hx0 = max(T.x0 - 1, 0), hx1 = min(T.xe, nx - 1);
+    const int hy0 = max(T.y0 - 1, 0), hy1 = min(T.ye, ny - 1);
+    const int hz0 = max(T.z0 - 1, 0), hz1 = min(T.ze, nz - 1);
+    const int rows_y = hy1 - hy0 + 1, rows = rows_y * (hz1 - hz0 + 1);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const float inv_h = P.inv_h;
+    const float o0 = P.origin[0], o1 = P.origin[1], o2 = P.origin[2];
+    for (int row = warp; row < rows; row += nwarps) {
+        const int cy = hy0 + row % rows_y, cz = hz0 + row / rows_y;
+        const uint32_t c0 = (uint32_t)hx0 + P.nx * ((uint32_t)cy + P.ny * (uint32_t)cz);
+        const uint32_t c1 = c0 + (uint32_t)(hx1 - hx0);
+        const uint32_t pbeg = b.offsets[c0];
+        const uint32_t pend = b.offsets[c1] + b.counts[c1];
+        for (uint32_t pp = pbeg + lane; pp < pend; pp += 32) {
+            const float4 pos = b.part_sorted[2 * (size_t)pp];
+            if (pos.w != 0.0f) continue;  // stray: handled by k_p2g_strays
+            const float4 vel = b.part_sorted[2 * (size_t)pp + 1];
+            const float q[3] = {__fmul_rn(__fsub_rn(pos.x, o0), inv_h), __fmul_rn(__fsub_rn(pos.y, o1), inv_h),
+                                __fmul_rn(__fsub_rn(pos.z, o2), inv_h)};
+            p2g_component(P, T, 0, q, vel.x, s_num[0], s_den[0]);
+            p2g_component(P, T, 1, q, vel.y, s_num[1], s_den[1]);
+            p2g_component(P, T, 2, q, vel.z, s_num[2], s_den[2]);
+        }
+    }
+    __syncthreads();
+
+    // Write every owned face once.
+    for (int axis = 0; axis < 3; axis++) {
+        const int sx = TILE + (axis == 0), sy = TILE + (axis == 1), sz = TILE + (axis == 2);
+        int lo[3], hi[3];
+        for (int bb = 0; bb < 3; bb++) owned_range(T, axis, bb, lo[bb], hi[bb]);
+        const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
+        for (int li = threadIdx.x; li < sx * sy * sz; li += blockDim.x) {
+            const int lx = li % sx, ly = (li / sx) % sy, lz = li / (sx * sy);
+            const int fi = T.x0 + lx, fj = T.y0 + ly, fk = T.z0 + lz;
+            if (fi >= hi[0] || fj >= hi[1] || fk >= hi[2]) continue;
+            const size_t gidx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
+            b.num[axis][gidx] = s_num[axis][li];
+            b.den[axis][gidx] = s_den[axis][li];
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_p2g_strays(DevBufs b) {
+    const DevParams& P = *b.prm;
+    const uint32_t ns = b.st->strays;
+    const int n3[3] = {(int)P.nx, (int)P.ny, (int)P.nz};
+    for (uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < ns; s += gridDim.x * blockDim.x) {
+        const uint32_t d = b.stray_list[s];
+        const float4 pos = b.part_sorted[2 * (size_t)d];
+        const float4 vel = b.part_sorted[2 * (size_t)d + 1];
+        const float q[3] = {__fmul_rn(__fsub_rn(pos.x, P.origin[0]), P.inv_h),
+                            __fmul_rn(__fsub_rn(pos.y, P.origin[1]), P.inv_h),
+                            __fmul_rn(__fsub_rn(pos.z, P.origin[2]), P.inv_h)};
+        const float vc[3] = {vel.x, vel.y, vel.z};
+        for (int axis = 0; axis < 3; axis++) {
+            int dim[3];
+            float t[3];
+            int base[3];
+            for (int bb = 0; bb < 3; bb++) {
+                dim[bb] = n3[bb] + (axis == bb ? 1 : 0);
+                const float g = __fadd_rn(q[bb], bb == axis ? 0.0f : -0.5f);
+                base[bb] = floor_to_i32(g);
+                t[bb] = __fsub_rn(g, (float)base[bb]);
+            }
+            for (int dk = 0; dk < 2; dk++) {
+                const int kk = base[2] + dk;
+                if (kk < 0 || kk >= dim[2]) continue;
+                const float wz = tent(t[2], dk);
+                for (int dj = 0; dj < 2; dj++) {
+                    const int jj = base[1] + dj;
+                    if (jj < 0 || jj >= dim[1]) continue;
+                    const float wy = tent(t[1], dj);
+                    for (int di = 0; di < 2; di++) {
+                        const int ii = base[0] + di;
+                        if (ii < 0 || ii >= dim[0]) continue;
+                        const float wx = tent(t[0], di);
+                        const float w = __fmul_rn(__fmul_rn(wx, wy), wz);
+                        if (w <= 0.0f) continue;
+                        const size_t idx = (size_t)ii + (size_t)dim[0] * ((size_t)jj + (size_t)dim[1] * kk);
+                        atomicAdd(&b.num[axis][idx], fixed_round(__fmul_rn(__fmul_rn(w, vc[axis]), P.fixed_scale)));
+                        atomicAdd(&b.den[axis][idx], fixed_round(__fmul_rn(w, P.fixed_scale)));
+                    }
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// grid prep
+
+// One face after normalize -> save_vel -> forces -> boundaries.
+// Returns the pre-force (saved) value in *saved.
+__device__ __forceinline__ float face_pre(const DevBufs& b, const DevParams& P, int axis, uint32_t fi,
+                                          uint32_t fj, uint32_t fk, float* saved) {
+    const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
+    const size_t idx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
+    const int32_t dn = b.den[axis][idx];
+    float v = 0.0f;
+    if (dn > 0) v = __fdiv_rn(__int2float_rn(b.num[axis][idx]), __int2float_rn(dn));  // normalize.wgsl:21-26
+    *saved = v;                                                                          // save_vel.wgsl:18
+    const uint32_t comp = axis == 0 ? fi : (axis == 1 ? fj : fk);
+    const uint32_t nax = axis == 0 ? P.nx : (axis == 1 ? P.ny : P.nz);
+    const size_t hi_c = (size_t)fi + P.nx * ((size_t)fj + (size_t)P.ny * fk);
+    const size_t step = axis == 0 ? 1 : (axis == 1 ? P.nx : (size_t)P.nx * P.ny);
+    const uint8_t tl = comp > 0 ? b.ct[hi_c - step] : CELL_SOLID;
+    const uint8_t th = comp < nax ? b.ct[hi_c] : CELL_SOLID;
+    const bool wet = (comp > 0 && tl == CELL_LIQUID) || (comp < nax && th == CELL_LIQUID);
+    if (wet) v = __fadd_rn(v, __fmul_rn(P.grav[axis], P.dt));      // forces.wgsl:75-83
+    if (comp == 0 || comp == nax || tl == CELL_SOLID || th == CELL_SOLID) v = 0.0f;  // boundaries.wgsl:43-60
+    return v;
+}
+
+__device__ __forceinline__ void face_out(const DevBufs& b, const DevParams& P, int axis, uint32_t fi, uint32_t fj,
+                                         uint32_t fk, float* v_out) {
+    float sv;
+    const float v = face_pre(b, P, axis, fi, fj, fk, &sv);
+    const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
+    const size_t idx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
+    b.vel[axis][idx] = v;
+    b.sav[axis][idx] = sv;
+    if (v_out) *v_out = v;
+}
+
+// cg_reduce.wgsl:38-49 tree over a 256-thread block (s has 256 floats).
+// Steps 128/64/32 go through shared memory, 16..1 through shuffles of warp 0;
+// the pairing (i with i+off) is the same at every level.
+__device__ __forceinline__ float block_tree256(float prod, float* s) {
+    const int t = threadIdx.x;
+    s[t] = prod;
+    __syncthreads();
+    if (t < 128) s[t] = __fadd_rn(s[t], s[t + 128]);
+    __syncthreads();
+    if (t < 64) s[t] = __fadd_rn(s[t], s[t + 64]);
+    __syncthreads();
+    float v = 0.0f;
+    if (t < 32) {
+        v = __fadd_rn(s[t], s[t + 32]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+    }
+    return v;
+}
+
+// (A x)_c of cg_spmv.wgsl:46-68 / cg_init.wgsl:24-48, neighbour order -x,+x,-y,+y,-z,+z.
+__device__ __forceinline__ float apply_A(const uint8_t* ct, const float* x, size_t c, size_t nx, size_t nxy, float xc) {
+    float cnt = 0.0f, sum = 0.0f;
+    const size_t nb[6] = {c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+        const uint8_t t = ct[nb[s]];
+        if (t != CELL_SOLID) {
+            cnt = __fadd_rn(cnt, 1.0f);
+            if (t == CELL_LIQUID) sum = __fadd_rn(sum, x[nb[s]]);
+        }
+    }
+    return __fsub_rn(__fmul_rn(cnt, xc), sum);
+}
+
+__global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
+    __shared__ float s_tree[256];
+    __shared__ double s_red[8];
+    const DevParams& P = *b.prm;
+    const uint32_t chunk = blockIdx.x;
+    const uint32_t c = chunk * 256 + threadIdx.x;
+    bool liquid = false;
+    float prod = 0.0f;
+    double prod64 = 0.0;
+    if (c < C) {
+        const uint32_t nx = P.nx, ny = P.ny, nz = P.nz;
+        const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+        float ul, vl, wl;
+        face_out(b, P, 0, i, j, k, &ul);
+        face_out(b, P, 1, i, j, k, &vl);
+        face_out(b, P, 2, i, j, k, &wl);
+        if (i == nx - 1) face_out(b, P, 0, nx, j, k, nullptr);
+        if (j == ny - 1) face_out(b, P, 1, i, ny, k, nullptr);
+        if (k == nz - 1) face_out(b, P, 2, i, j, nz, nullptr);
+        liquid = b.ct[c] == CELL_LIQUID;
+        if (liquid) {
+            // divergence.wgsl:36-58 (liquid cells are interior, so i+1 <= nx-1)
+            float sv;
+            const float uh = face_pre(b, P, 0, i + 1, j, k, &sv);
+            const float vh = face_pre(b, P, 1, i, j + 1, k, &sv);
+            const float wh = face_pre(b, P, 2, i, j, k + 1, &sv);
+            float dv = __fmul_rn(__fadd_rn(__fadd_rn(__fsub_rn(uh, ul), __fsub_rn(vh, vl)), __fsub_rn(wh, wl)), P.inv_h);
+            if (P.stiff > 0.0f && P.rest > 0.0f) {
+                const float over = __fdiv_rn(fmaxf(0.0f, __fsub_rn(__uint2float_rn(b.counts[c]), P.rest)), P.rest);
+                const float drift = fminf(__fmul_rn(P.stiff, over), P.drift_clamp);
+                dv = __fsub_rn(dv, drift);
+            }
+            // cg_init.wgsl:66-81
+            const float rhs = __fmul_rn(-P.scale_rhs, dv);
+            float ap = 0.0f;
+            if (P.warm) {
+                const float p_initial = b.p[c];
+                ap = apply_A(b.ct, b.p, c, nx, (size_t)nx * ny, p_initial);
+            } else {
+                b.p[c] = 0.0f;
+            }
+            const float rc = __fsub_rn(rhs, ap);
+            b.r[c] = rc;
+            b.dA[c] = rc;
+            prod = __fmul_rn(rc, rc);
+            prod64 = (double)rc * (double)rc;
+        } else {
+            b.p[c] = 0.0f;
+            b.r[c] = 0.0f;
+            b.dA[c] = 0.0f;
+        }
+    }
+    const int any = __syncthreads_or(liquid);
+    const float v = block_tree256(prod, s_tree);
+    // f64 partial of this chunk (fixed order: warp shuffles, then warps in order)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) prod64 += __shfl_down_sync(0xffffffffu, prod64, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = prod64;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int w = 0; w < 8; w++) a += s_red[w];
+        b.part_rr[chunk] = v;
+        b.part_dq[chunk] = 0.0f;
+        b.chunk_rr64[chunk] = a;
+        b.chunk_flag[chunk] = any ? 1 : 0;
+    }
+}
+
+__device__ __forceinline__ void face_project(const DevBufs& b, const DevParams& P, int axis, uint32_t fi,
+                                             uint32_t fj, uint32_t fk) {
+    const uint32_t comp = axis == 0 ? fi : (axis == 1 ? fj : fk);
+    const uint32_t nax = axis == 0 ? P.nx : (axis == 1 ? P.ny : P.nz);
+    if (comp == 0 || comp == nax) return;  // gradient.wgsl:45
+    const size_t hi = (size_t)fi + P.nx * ((size_t)fj + (size_t)P.ny * fk);
+    const size_t lo = hi - (axis == 0 ? 1 : (axis == 1 ? P.nx : (size_t)P.nx * P.ny));
+    const uint8_t lt = b.ct[lo], ht = b.ct[hi];
+    if (lt == CELL_SOLID || ht == CELL_SOLID) return;
+    if (lt != CELL_LIQUID && ht != CELL_LIQUID) return;
+    const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
+    const size_t idx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
+    const float dp = __fsub_rn(b.p[hi], b.p[lo]);
+    b.vel[axis][idx] = __fsub_rn(b.vel[axis][idx], __fmul_rn(P.coeff_grad, dp));
+}
+
+__global__ void __launch_bounds__(256) k_project(DevBufs b, uint32_t C) {
+    const DevParams& P = *b.prm;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= C) return;
+    const uint32_t nx = P.nx, ny = P.ny;
+    const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+    face_project(b, P, 0, i, j, k);
+    face_project(b, P, 1, i, j, k);
+    face_project(b, P, 2, i, j, k);
+}
+
+// Stand-alone solve: cg_init.wgsl:50-87 from a given divergence field (the
+// tail of k_grid_prep without the face passes).
+__global__ void __launch_bounds__(256) k_solve_init(DevBufs b, uint32_t C, const float* __restrict__ div) {
+    __shared__ float s_tree[256];
+    __shared__ double s_red[8];
+    const DevParams& P = *b.prm;
+    const uint32_t chunk = blockIdx.x;
+    const uint32_t c = chunk * 256 + threadIdx.x;
+    bool liquid = false;
+    float prod = 0.0f;
+    double prod64 = 0.0;
+    if (c < C) {
+        liquid = b.ct[c] == CELL_LIQUID;
+        if (liquid) {
+            const float rhs = __fmul_rn(-P.scale_rhs, div[c]);
+            float ap = 0.0f;
+            if (P.warm) {
+                const float p_initial = b.p[c];
+                ap = apply_A(b.ct, b.p, c, P.nx, (size_t)P.nx * P.ny, p_initial);
+            } else {
+                b.p[c] = 0.0f;
+            }
+            const float rc = __fsub_rn(rhs, ap);
+            b.r[c] = rc;
+            b.dA[c] = rc;
+            prod = __fmul_rn(rc, rc);
+            prod64 = (double)rc * (double)rc;
+        } else {
+            b.p[c] = 0.0f;
+            b.r[c] = 0.0f;
+            b.dA[c] = 0.0f;
+        }
+    }
+    const int any = __syncthreads_or(liquid);
+    const float v = block_tree256(prod, s_tree);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) prod64 += __shfl_down_sync(0xffffffffu, prod64, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = prod64;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0;
+        for (int w = 0; w < 8; w++) a += s_red[w];
+        b.part_rr[chunk] = v;
+        b.part_dq[chunk] = 0.0f;
+        b.chunk_rr64[chunk] = a;
+        b.chunk_flag[chunk] = any ? 1 : 0;
+    }
+}
+
+cudaError_t launch_solve_init(const DevBufs& b, uint32_t C, const float* div, cudaStream_t s) {
+    k_solve_init<<<(C + 255) / 256, 256, 0, s>>>(b, C, div);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s) {
+    k_classify<<<(C + 255) / 256, 256, 0, s>>>(b, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s) {
+    const int tx = (int)((nx + TILE - 1) / TILE), ty = (int)((ny + TILE - 1) / TILE), tz = (int)((nz + TILE - 1) / TILE);
+    k_p2g_tile<<<tx * ty * tz, 256, 0, s>>>(b, tx, ty);
+    k_p2g_strays<<<L.num_sms, 256, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_grid_prep(const DevBufs& b, uint32_t C, cudaStream_t s) {
+    k_grid_prep<<<(C + 255) / 256, 256, 0, s>>>(b, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_project(const DevBufs& b, uint32_t C, cudaStream_t s) {
+    k_project<<<(C + 255) / 256, 256, 0, s>>>(b, C);
+    return cudaGetLastError();
+}
+
+}  // namespace fl

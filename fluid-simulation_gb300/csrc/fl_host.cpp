@@ -1,0 +1,781 @@
+// fl_host.cpp — C ABI of the FLIP/PIC substep (include/fluidgb.h).
+//
+// A handle owns one device pool holding every buffer of the step, a stream,
+// and a CUDA graph of one substep (the reference records one command encoder
+// per substep, gpu/mod.rs:973-982; here the whole substep replays as one graph
+// launch).  Settings live in device memory, so live parameter changes
+// (fluid.rs:1294-1371) never invalidate the graph.
+//
+// This file is compiled with -ffp-contract=off: the derived scalars below are
+// evaluated in f32 in the shaders' operation order.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fluidgb.h"
+#include "fl_device.cuh"
+
+using fl::DevBufs;
+using fl::DevParams;
+using fl::DevStats;
+
+struct fl_handle {
+    fl_params prm;
+    uint32_t nx = 0, ny = 0, nz = 0, C = 0, F3[3] = {0, 0, 0}, nchunks = 0;
+    uint32_t cap = 0, n = 0;
+    int device = 0;
+    fl::LaunchCfg L{};
+    DevParams hp{};
+    DevBufs b{};
+    void* pool = nullptr;
+    size_t pool_bytes = 0;
+    float4* partA = nullptr;
+    uint32_t* idsA = nullptr;
+    DevParams* dprm = nullptr;
+    DevStats* dst = nullptr;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaGraphExec_t graph = nullptr;
+    bool graph_failed = false;
+    bool profiling = false;
+    cudaEvent_t ev[FL_STAGE_COUNT + 1] = {};
+    double stage_ms[FL_STAGE_COUNT] = {};
+    uint64_t stage_steps = 0;
+    std::vector<float> init_part;
+    uint32_t init_n = 0;
+    uint64_t substeps = 0;
+    std::string err;
+};
+
+namespace {
+
+thread_local std::string g_err;
+
+fl_status set_err(fl_handle* h, fl_status s, const std::string& msg) {
+    if (h)
+        h->err = msg;
+    else
+        g_err = msg;
+    return s;
+}
+
+fl_status cuda_err(fl_handle* h, cudaError_t e, const char* what) {
+    return set_err(h, FL_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define FL_CUDA(h, call)                                        \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_err((h), e_, #call); \
+    } while (0)
+
+uint32_t f2u_sat(float x) {
+    if (!(x > 0.0f)) return 0u;
+    if (x >= 4294967296.0f) return 0xffffffffu;
+    return (uint32_t)x;
+}
+
+fl_status validate(const fl_params* p, std::string* why) {
+    if (!p) { *why = "params is NULL"; return FL_INVALID_ARG; }
+    if (p->gdim[0] < 3 || p->gdim[1] < 3 || p->gdim[2] < 3) { *why = "each grid dimension must be >= 3"; return FL_INVALID_ARG; }
+    if (p->gdim[0] > 2048 || p->gdim[1] > 2048 || p->gdim[2] > 2048) { *why = "grid dimension > 2048"; return FL_INVALID_ARG; }
+    if ((uint64_t)p->gdim[0] * p->gdim[1] * p->gdim[2] > (1ull << 30)) { *why = "more than 2^30 cells"; return FL_INVALID_ARG; }
+    if (!(p->geom[0] > 0.0f) || !(p->geom[1] > 0.0f)) { *why = "h and inv_h must be > 0"; return FL_INVALID_ARG; }
+    if (!(p->geom[2] > 0.0f)) { *why = "dt must be > 0"; return FL_INVALID_ARG; }
+    if (!(p->phys[1] > 0.0f)) { *why = "rho must be > 0"; return FL_INVALID_ARG; }
+    if (p->cg_precision > 1u) { *why = "cg_precision must be FL_CG_F32 or FL_CG_F64"; return FL_INVALID_ARG; }
+    if (p->advect_order > 2u) { *why = "advect_order must be 1 or 2"; return FL_INVALID_ARG; }
+    for (int i = 0; i < 4; i++)
+        if (p->reserved[i]) { *why = "reserved fields must be zero"; return FL_INVALID_ARG; }
+    return FL_OK;
+}
+
+// Derived settings, in the shaders' f32 operation order.
+void derive(const fl_params& p, uint32_t n, DevParams& d) {
+    d = DevParams{};
+    d.nx = p.gdim[0]; d.ny = p.gdim[1]; d.nz = p.gdim[2];
+    d.C = d.nx * d.ny * d.nz;
+    d.F3[0] = (d.nx + 1) * d.ny * d.nz;
+    d.F3[1] = d.nx * (d.ny + 1) * d.nz;
+    d.F3[2] = d.nx * d.ny * (d.nz + 1);
+    d.n = n;
+    d.h = p.geom[0]; d.inv_h = p.geom[1]; d.dt = p.geom[2]; d.fixed_scale = p.geom[3];
+    d.rho = p.phys[1]; d.flip = p.phys[2]; d.friction = p.phys[3];
+    const float cfl = std::fmax(p.cls[2], 1.0f);                 // g2p.wgsl:159
+    d.maxs = cfl * d.h / d.dt;                                    // g2p.wgsl:160
+    for (int a = 0; a < 3; a++) { d.origin[a] = p.origin[a]; d.grav[a] = p.grav[a]; }
+    d.scale_rhs = d.rho * d.h * d.h / d.dt;                       // cg_init.wgsl:68
+    d.coeff_grad = (d.dt / d.rho) / d.h;                          // gradient.wgsl:65
+    d.rest = p.spc[0]; d.stiff = p.spc[1]; d.drift_clamp = p.spc[2];
+    const float tolc = std::fmin(std::fmax(p.pressure_tolerance, 0.0f), 0.1f);  // fluid.rs:47-50
+    d.tol_sq = tolc * tolc;
+    d.tol_sq_d = (double)tolc * (double)tolc;
+    const uint32_t nn[3] = {d.nx, d.ny, d.nz};
+    for (int a = 0; a < 3; a++) {
+        const float extent = (float)nn[a] * d.h;                  // g2p.wgsl:165
+        d.lo[a] = d.origin[a] + d.h * 1.05f;                      // g2p.wgsl:166
+        d.hi[a] = d.origin[a] + extent - d.h * 1.05f;             // g2p.wgsl:167
+    }
+    d.half_dt = 0.5f * d.dt;
+    d.thresh = std::max(f2u_sat(p.cls[0]), 1u);                   // classify.wgsl:42
+    d.dilation = f2u_sat(p.cls[1]) >= 1u ? 1u : 0u;               // classify.wgsl:48
+    d.warm = p.dims[3] != 0u ? 1u : 0u;
+    d.iters = p.dims[2] ? p.dims[2] : 1u;                          // fluid.rs:286
+    d.precision = p.cg_precision;
+    d.advect_order = p.advect_order == 2u ? 2u : 1u;
+    d.nchunks = (d.C + fl::CHUNK - 1) / fl::CHUNK;
+}
+
+struct PoolPlan {
+    size_t off = 0;
+    template <class T>
+    size_t take(size_t count) {
+        off = (off + 255) & ~size_t(255);
+        const size_t o = off;
+        off += sizeof(T) * std::max<size_t>(count, 1);
+        return o;
+    }
+};
+
+int g_num_sms = -1;
+int g_cg_per_sm = 0;
+
+fl_status device_check(fl_handle* h) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return set_err(h, FL_NO_DEVICE, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, dev);
+    if (e != cudaSuccess) return set_err(h, FL_NO_DEVICE, std::string("cudaGetDeviceProperties: ") + cudaGetErrorString(e));
+    if (!(prop.major == 10 && prop.minor == 3))
+        return set_err(h, FL_NO_DEVICE, "this build targets sm_103a (GB300); found sm_" + std::to_string(prop.major) +
+                                            std::to_string(prop.minor));
+    if (!prop.cooperativeLaunch) return set_err(h, FL_NO_DEVICE, "device does not support cooperative launch");
+    g_num_sms = prop.multiProcessorCount;
+    g_cg_per_sm = fl::cg_max_blocks_per_sm();
+    if (g_cg_per_sm < 1) return set_err(h, FL_INTERNAL, "CG kernel cannot be resident (occupancy 0)");
+    return FL_OK;
+}
+
+fl::LaunchCfg make_cfg(uint32_t nchunks) {
+    fl::LaunchCfg L;
+    L.num_sms = g_num_sms;
+    const int max_cg = g_num_sms * g_cg_per_sm;
+    const int want = (int)((nchunks + fl::CG_GROUPS - 1) / fl::CG_GROUPS);
+    L.cg_blocks = std::max(1, std::min(max_cg, want));
+    L.particle_blocks = g_num_sms * 8;
+    return L;
+}
+
+// Enqueue one substep.  The caller set b.part_in/out/ids.  With `ev`, an
+// event is recorded before the first stage and after every stage.
+cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEvent_t* ev = nullptr) {
+    cudaError_t e;
+    auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
+    if ((e = cudaMemsetAsync(h->dst, 0, fl::DEVSTATS_STEP_BYTES, s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(b.counts, 0, sizeof(uint32_t) * (size_t)h->C, s)) != cudaSuccess) return e;
+    if ((e = mark(0)) != cudaSuccess) return e;
+    if ((e = fl::launch_bin(b, h->L, h->C, h->cap, s)) != cudaSuccess) return e;
+    if ((e = mark(1)) != cudaSuccess) return e;
+    if ((e = fl::launch_classify(b, h->C, s)) != cudaSuccess) return e;
+    if ((e = mark(2)) != cudaSuccess) return e;
+    if ((e = fl::launch_p2g(b, h->L, h->nx, h->ny, h->nz, s)) != cudaSuccess) return e;
+    if ((e = mark(3)) != cudaSuccess) return e;
+    if ((e = fl::launch_grid_prep(b, h->C, s)) != cudaSuccess) return e;
+    if ((e = mark(4)) != cudaSuccess) return e;
+    if ((e = fl::launch_cg(b, h->L, s)) != cudaSuccess) return e;
+    if ((e = mark(5)) != cudaSuccess) return e;
+    if ((e = fl::launch_project(b, h->C, s)) != cudaSuccess) return e;
+    if ((e = mark(6)) != cudaSuccess) return e;
+    if ((e = fl::launch_g2p(b, h->L, s)) != cudaSuccess) return e;
+    if ((e = mark(7)) != cudaSuccess) return e;
+    return cudaSuccess;
+}
+
+fl_status upload_params(fl_handle* h) {
+    derive(h->prm, h->n, h->hp);
+    FL_CUDA(h, cudaMemcpyAsync(h->dprm, &h->hp, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
+    return FL_OK;
+}
+
+fl_status read_status(fl_handle* h) {
+    uint32_t st = 0;
+    FL_CUDA(h, cudaMemcpyAsync(&st, &h->dst->status, 4, cudaMemcpyDeviceToHost, h->stream));
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (st != 0u) {
+        const uint32_t zero = 0;
+        FL_CUDA(h, cudaMemcpyAsync(&h->dst->status, &zero, 4, cudaMemcpyHostToDevice, h->stream));
+        FL_CUDA(h, cudaStreamSynchronize(h->stream));
+        return set_err(h, (fl_status)st, "a device-side wait expired (status " + std::to_string(st) + ")");
+    }
+    return FL_OK;
+}
+
+fl_status build_graph(fl_handle* h) {
+    if (h->graph || h->graph_failed) return FL_OK;
+    DevBufs b = h->b;
+    b.part_in = h->partA;
+    b.part_out = h->partA;
+    b.ids_in = h->idsA;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(h->own_stream, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        cudaError_t le = enqueue_step(h, b, h->own_stream);
+        e = cudaStreamEndCapture(h->own_stream, &g);
+        if (le != cudaSuccess) e = le;
+    }
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&h->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        // Fall back to direct launches; clear the sticky capture error.
+        h->graph = nullptr;
+        h->graph_failed = true;
+        (void)cudaGetLastError();
+    }
+    return FL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t fl_abi_version(void) { return FL_ABI_VERSION; }
+
+const char* fl_status_string(fl_status s) {
+    switch (s) {
+        case FL_OK: return "FL_OK";
+        case FL_INVALID_ARG: return "FL_INVALID_ARG";
+        case FL_OOM: return "FL_OOM";
+        case FL_CUDA_ERROR: return "FL_CUDA_ERROR";
+        case FL_NOT_CONVERGED: return "FL_NOT_CONVERGED";
+        case FL_TIMEOUT: return "FL_TIMEOUT";
+        case FL_NO_DEVICE: return "FL_NO_DEVICE";
+        case FL_INTERNAL: return "FL_INTERNAL";
+    }
+    return "FL_UNKNOWN";
+}
+
+fl_status fl_params_default(fl_params* out, uint32_t nx, uint32_t ny, uint32_t nz, float h, const float* origin) {
+    if (!out) return set_err(nullptr, FL_INVALID_ARG, "out is NULL");
+    if (!(h > 0.0f)) return set_err(nullptr, FL_INVALID_ARG, "h must be > 0");
+    std::memset(out, 0, sizeof(*out));
+    // Registry defaults, app/crates/fluid-lab/src/settings/mod.rs:498-724.
+    out->dims[0] = nx;
+    out->dims[1] = 0;
+    out->dims[2] = 30;   // solver.pressure_iterations
+    out->dims[3] = 1;    // solver.pressure_warm_start
+    out->geom[0] = h;
+    out->geom[1] = 1.0f / h;
+    out->geom[2] = 1.0f / 120.0f;  // physics.fixed_dt
+    out->geom[3] = 65536.0f;       // FIXED_SCALE (fluid.rs:41)
+    out->phys[0] = -9.81f;         // physics.gravity
+    out->phys[1] = 1000.0f;        // rho (fluid.rs:299)
+    out->phys[2] = 0.9f;           // physics.flip_blend
+    out->phys[3] = 0.0f;           // physics.wall_friction
+    const uint32_t nn[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; a++) out->origin[a] = origin ? origin[a] : -(float)nn[a] * h / 2.0f;  // fluid.rs:262-266
+    out->grav[1] = -9.81f;
+    out->spc[0] = 8.0f;            // effective rest density at the reference particle density
+    out->spc[1] = 0.45f;           // physics.volume_stiffness
+    out->spc[2] = 0.5f;            // physics.drift_clamp
+    out->cls[0] = 1.0f;            // classify.liquid_threshold
+    out->cls[1] = 0.0f;            // classify.surface_dilation
+    out->cls[2] = 2.0f;            // physics.cfl
+    out->gdim[0] = nx; out->gdim[1] = ny; out->gdim[2] = nz;
+    out->pressure_tolerance = 0.0f;  // solver.pressure_residual_tolerance
+    out->cg_precision = FL_CG_F32;
+    out->advect_order = 1;
+    out->sort_period = 4;            // dev.particle_sort_period
+    return FL_OK;
+}
+
+fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out) {
+    if (!out) return set_err(nullptr, FL_INVALID_ARG, "out is NULL");
+    *out = nullptr;
+    std::string why;
+    if (validate(params, &why) != FL_OK) return set_err(nullptr, FL_INVALID_ARG, why);
+    fl_status s = device_check(nullptr);
+    if (s != FL_OK) return s;
+    fl_handle* h = new (std::nothrow) fl_handle();
+    if (!h) return set_err(nullptr, FL_OOM, "host allocation failed");
+    h->prm = *params;
+    h->nx = params->gdim[0]; h->ny = params->gdim[1]; h->nz = params->gdim[2];
+    h->C = h->nx * h->ny * h->nz;
+    h->F3[0] = (h->nx + 1) * h->ny * h->nz;
+    h->F3[1] = h->nx * (h->ny + 1) * h->nz;
+    h->F3[2] = h->nx * h->ny * (h->nz + 1);
+    h->nchunks = (h->C + fl::CHUNK - 1) / fl::CHUNK;
+    h->cap = capacity;
+    cudaGetDevice(&h->device);
+    h->L = make_cfg(h->nchunks);
+
+    const size_t cap = std::max<uint32_t>(capacity, 1);
+    const size_t C = h->C;
+    const uint32_t nb = (h->C + fl::SCAN_TILE - 1) / fl::SCAN_TILE;
+    PoolPlan pl;
+    size_t o_partA = pl.take<float4>(2 * cap), o_partB = pl.take<float4>(2 * cap);
+    size_t o_idsA = pl.take<uint32_t>(cap), o_idsB = pl.take<uint32_t>(cap);
+    size_t o_keys = pl.take<uint32_t>(cap), o_perm = pl.take<uint32_t>(cap);
+    size_t o_scr = pl.take<uint32_t>(cap), o_stray = pl.take<uint32_t>(cap);
+    size_t o_counts = pl.take<uint32_t>(C), o_offs = pl.take<uint32_t>(C), o_cur = pl.take<uint32_t>(C);
+    size_t o_spine = pl.take<uint32_t>(nb), o_big = pl.take<uint32_t>(C);
+    size_t o_ct = pl.take<uint8_t>(C), o_flag = pl.take<uint8_t>(h->nchunks);
+    size_t o_num[3], o_den[3], o_vel[3], o_sav[3];
+    for (int a = 0; a < 3; a++) {
+        o_num[a] = pl.take<int32_t>(h->F3[a]);
+        o_den[a] = pl.take<int32_t>(h->F3[a]);
+        o_vel[a] = pl.take<float>(h->F3[a]);
+        o_sav[a] = pl.take<float>(h->F3[a]);
+    }
+    size_t o_p = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C), o_dB = pl.take<float>(C),
+           o_q = pl.take<float>(C);
+    size_t o_prr = pl.take<float>(h->nchunks), o_pdq = pl.take<float>(h->nchunks);
+    size_t o_c64 = pl.take<double>(h->nchunks);
+    size_t o_cta = pl.take<double>(2 * (size_t)g_num_sms * g_cg_per_sm);
+    size_t o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
+    h->pool_bytes = pl.off;
+
+    cudaError_t e = cudaMalloc(&h->pool, h->pool_bytes);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        delete h;
+        return set_err(nullptr, FL_OOM, "cudaMalloc of " + std::to_string(h->pool_bytes) + " bytes failed");
+    }
+    char* base = (char*)h->pool;
+    if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        cudaFree(h->pool);
+        delete h;
+        return cuda_err(nullptr, e, "cudaStreamCreate");
+    }
+    h->stream = h->own_stream;
+    if ((e = cudaMemsetAsync(h->pool, 0, h->pool_bytes, h->stream)) != cudaSuccess) {
+        fl_destroy(h);
+        return cuda_err(nullptr, e, "cudaMemset");
+    }
+    DevBufs& b = h->b;
+    h->partA = (float4*)(base + o_partA);
+    h->idsA = (uint32_t*)(base + o_idsA);
+    h->dprm = (DevParams*)(base + o_prm);
+    h->dst = (DevStats*)(base + o_st);
+    b.prm = h->dprm;
+    b.st = h->dst;
+    b.part_in = h->partA;
+    b.part_sorted = (float4*)(base + o_partB);
+    b.part_out = h->partA;
+    b.ids_in = h->idsA;
+    b.ids_sorted = (uint32_t*)(base + o_idsB);
+    b.keys = (uint32_t*)(base + o_keys);
+    b.perm = (uint32_t*)(base + o_perm);
+    b.scratch_u32 = (uint32_t*)(base + o_scr);
+    b.stray_list = (uint32_t*)(base + o_stray);
+    b.counts = (uint32_t*)(base + o_counts);
+    b.offsets = (uint32_t*)(base + o_offs);
+    b.cursor = (uint32_t*)(base + o_cur);
+    b.spine = (uint32_t*)(base + o_spine);
+    b.big_list = (uint32_t*)(base + o_big);
+    b.ct = (uint8_t*)(base + o_ct);
+    b.chunk_flag = (uint8_t*)(base + o_flag);
+    for (int a = 0; a < 3; a++) {
+        b.num[a] = (int32_t*)(base + o_num[a]);
+        b.den[a] = (int32_t*)(base + o_den[a]);
+        b.vel[a] = (float*)(base + o_vel[a]);
+        b.sav[a] = (float*)(base + o_sav[a]);
+    }
+    b.p = (float*)(base + o_p);
+    b.r = (float*)(base + o_r);
+    b.dA = (float*)(base + o_dA);
+    b.dB = (float*)(base + o_dB);
+    b.q = (float*)(base + o_q);
+    b.part_rr = (float*)(base + o_prr);
+    b.part_dq = (float*)(base + o_pdq);
+    b.chunk_rr64 = (double*)(base + o_c64);
+    b.cta_part64 = (double*)(base + o_cta);
+    if ((s = upload_params(h)) != FL_OK) {
+        std::string m = h->err;
+        fl_destroy(h);
+        return set_err(nullptr, s, m);
+    }
+    *out = h;
+    return FL_OK;
+}
+
+fl_status fl_destroy(fl_handle* h) {
+    if (!h) return FL_OK;
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    for (int k = 0; k <= FL_STAGE_COUNT; k++)
+        if (h->ev[k]) cudaEventDestroy(h->ev[k]);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    if (h->pool) cudaFree(h->pool);
+    delete h;
+    return FL_OK;
+}
+
+fl_status fl_set_params(fl_handle* h, const fl_params* params) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    std::string why;
+    if (validate(params, &why) != FL_OK) return set_err(h, FL_INVALID_ARG, why);
+    if (params->gdim[0] != h->nx || params->gdim[1] != h->ny || params->gdim[2] != h->nz)
+        return set_err(h, FL_INVALID_ARG, "grid dimensions cannot change on a live handle; create a new one");
+    h->prm = *params;
+    return upload_params(h);
+}
+
+fl_status fl_get_params(const fl_handle* h, fl_params* out) {
+    if (!h || !out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    *out = h->prm;
+    out->dims[1] = h->n;
+    return FL_OK;
+}
+
+fl_status fl_set_particles(fl_handle* h, const float* aos, uint32_t n) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (n > h->cap) return set_err(h, FL_INVALID_ARG, "n exceeds the handle capacity");
+    if (n && !aos) return set_err(h, FL_INVALID_ARG, "particles is NULL");
+    h->init_part.assign(aos, aos + (size_t)n * 8);
+    h->init_n = n;
+    return fl_reset(h);
+}
+
+fl_status fl_get_particles(fl_handle* h, float* out, uint32_t* ids) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (out && h->n)
+        FL_CUDA(h, cudaMemcpyAsync(out, h->partA, (size_t)h->n * 32, cudaMemcpyDeviceToHost, h->stream));
+    if (ids && h->n) FL_CUDA(h, cudaMemcpyAsync(ids, h->idsA, (size_t)h->n * 4, cudaMemcpyDeviceToHost, h->stream));
+    return read_status(h);
+}
+
+fl_status fl_particle_count(const fl_handle* h, uint32_t* n_out) {
+    if (!h || !n_out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    *n_out = h->n;
+    return FL_OK;
+}
+
+fl_status fl_step(fl_handle* h, uint32_t substeps) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (substeps == 0) return FL_OK;
+    build_graph(h);
+    for (uint32_t i = 0; i < substeps; i++) {
+        if (h->profiling) {
+            DevBufs b = h->b;
+            b.part_in = h->partA;
+            b.part_out = h->partA;
+            b.ids_in = h->idsA;
+            FL_CUDA(h, enqueue_step(h, b, h->stream, h->ev));
+            FL_CUDA(h, cudaEventSynchronize(h->ev[FL_STAGE_COUNT]));
+            for (int k = 0; k < FL_STAGE_COUNT; k++) {
+                float ms = 0.0f;
+                FL_CUDA(h, cudaEventElapsedTime(&ms, h->ev[k], h->ev[k + 1]));
+                h->stage_ms[k] += ms;
+            }
+            h->stage_steps++;
+        } else if (h->graph) {
+            FL_CUDA(h, cudaGraphLaunch(h->graph, h->stream));
+        } else {
+            DevBufs b = h->b;
+            b.part_in = h->partA;
+            b.part_out = h->partA;
+            b.ids_in = h->idsA;
+            FL_CUDA(h, enqueue_step(h, b, h->stream));
+        }
+        h->substeps++;
+    }
+    return FL_OK;
+}
+
+fl_status fl_step_device(fl_handle* h, void* particles_dev, uint32_t n) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (n > h->cap) return set_err(h, FL_INVALID_ARG, "n exceeds the handle capacity");
+    if (n && !particles_dev) return set_err(h, FL_INVALID_ARG, "particles_dev is NULL");
+    if (((uintptr_t)particles_dev & 15u) != 0) return set_err(h, FL_INVALID_ARG, "particles_dev must be 16-byte aligned");
+    cudaPointerAttributes attr;
+    cudaError_t e = cudaPointerGetAttributes(&attr, particles_dev);
+    if (e != cudaSuccess || (attr.type != cudaMemoryTypeDevice && attr.type != cudaMemoryTypeManaged)) {
+        (void)cudaGetLastError();
+        return set_err(h, FL_INVALID_ARG, "particles_dev is not a device pointer");
+    }
+    if (n != h->n) {
+        h->n = n;
+        fl_status s = upload_params(h);
+        if (s != FL_OK) return s;
+    }
+    DevBufs b = h->b;
+    b.part_in = (float4*)particles_dev;
+    b.part_out = (float4*)particles_dev;
+    b.ids_in = nullptr;
+    FL_CUDA(h, enqueue_step(h, b, h->stream));
+    h->substeps++;
+    return FL_OK;
+}
+
+fl_status fl_step_host(fl_handle* h, const float* in, float* out, uint32_t n, uint32_t substeps) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (n > h->cap) return set_err(h, FL_INVALID_ARG, "n exceeds the handle capacity");
+    if (n && (!in || !out)) return set_err(h, FL_INVALID_ARG, "particle buffer is NULL");
+    if (n) FL_CUDA(h, cudaMemcpyAsync(h->partA, in, (size_t)n * 32, cudaMemcpyHostToDevice, h->stream));
+    if (n != h->n) {
+        h->n = n;
+        fl_status s = upload_params(h);
+        if (s != FL_OK) return s;
+    }
+    fl_status s = fl_step(h, substeps);
+    if (s != FL_OK) return s;
+    if (n) FL_CUDA(h, cudaMemcpyAsync(out, h->partA, (size_t)n * 32, cudaMemcpyDeviceToHost, h->stream));
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return read_status(h);
+}
+
+fl_status fl_set_profiling(fl_handle* h, int enable) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (enable && !h->ev[0]) {
+        for (int k = 0; k <= FL_STAGE_COUNT; k++) FL_CUDA(h, cudaEventCreate(&h->ev[k]));
+    }
+    h->profiling = enable != 0;
+    return FL_OK;
+}
+
+fl_status fl_get_stage_times(fl_handle* h, double* ms_out, uint64_t* substeps_out) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (ms_out)
+        for (int k = 0; k < FL_STAGE_COUNT; k++) ms_out[k] = h->stage_ms[k];
+    if (substeps_out) *substeps_out = h->stage_steps;
+    return FL_OK;
+}
+
+fl_status fl_reset_stage_times(fl_handle* h) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    for (int k = 0; k < FL_STAGE_COUNT; k++) h->stage_ms[k] = 0.0;
+    h->stage_steps = 0;
+    return FL_OK;
+}
+
+fl_status fl_sync(fl_handle* h) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return read_status(h);
+}
+
+fl_status fl_set_stream(fl_handle* h, void* cuda_stream) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
+    return FL_OK;
+}
+
+fl_status fl_apply_impulse(fl_handle* h, const float dv[3]) {
+    if (!h || !dv) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    FL_CUDA(h, fl::launch_impulse(h->partA, h->dprm, dv[0], dv[1], dv[2], h->L, h->stream));
+    return FL_OK;
+}
+
+fl_status fl_reset(fl_handle* h) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    h->n = h->init_n;
+    if (h->n) {
+        FL_CUDA(h, cudaMemcpyAsync(h->partA, h->init_part.data(), (size_t)h->n * 32, cudaMemcpyHostToDevice, h->stream));
+        std::vector<uint32_t> ids(h->n);
+        for (uint32_t i = 0; i < h->n; i++) ids[i] = i;
+        FL_CUDA(h, cudaMemcpyAsync(h->idsA, ids.data(), (size_t)h->n * 4, cudaMemcpyHostToDevice, h->stream));
+        FL_CUDA(h, cudaStreamSynchronize(h->stream));  // `ids` is a local
+    }
+    FL_CUDA(h, cudaMemsetAsync(h->b.p, 0, sizeof(float) * (size_t)h->C, h->stream));
+    h->substeps = 0;
+    return upload_params(h);
+}
+
+fl_status fl_get_grid(fl_handle* h, const fl_grid_view* v) {
+    if (!h || !v) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    float* fd[6] = {v->u, v->v, v->w, v->u_saved, v->v_saved, v->w_saved};
+    for (int a = 0; a < 6; a++) {
+        if (!fd[a]) continue;
+        const float* src = a < 3 ? h->b.vel[a] : h->b.sav[a - 3];
+        FL_CUDA(h, cudaMemcpyAsync(fd[a], src, sizeof(float) * (size_t)h->F3[a % 3], cudaMemcpyDeviceToHost, h->stream));
+    }
+    const size_t C = h->C;
+    if (v->pressure) FL_CUDA(h, cudaMemcpyAsync(v->pressure, h->b.p, 4 * C, cudaMemcpyDeviceToHost, h->stream));
+    if (v->cell_type) FL_CUDA(h, cudaMemcpyAsync(v->cell_type, h->b.ct, C, cudaMemcpyDeviceToHost, h->stream));
+    if (v->counts) FL_CUDA(h, cudaMemcpyAsync(v->counts, h->b.counts, 4 * C, cudaMemcpyDeviceToHost, h->stream));
+    if (v->offsets) FL_CUDA(h, cudaMemcpyAsync(v->offsets, h->b.offsets, 4 * C, cudaMemcpyDeviceToHost, h->stream));
+    return read_status(h);
+}
+
+fl_status fl_get_bins(fl_handle* h, uint32_t* counts, uint32_t* offsets, uint32_t* perm) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    const size_t C = h->C;
+    if (counts) FL_CUDA(h, cudaMemcpyAsync(counts, h->b.counts, 4 * C, cudaMemcpyDeviceToHost, h->stream));
+    if (offsets) FL_CUDA(h, cudaMemcpyAsync(offsets, h->b.offsets, 4 * C, cudaMemcpyDeviceToHost, h->stream));
+    if (perm && h->n) FL_CUDA(h, cudaMemcpyAsync(perm, h->b.perm, 4 * (size_t)h->n, cudaMemcpyDeviceToHost, h->stream));
+    return read_status(h);
+}
+
+fl_status fl_get_stats(fl_handle* h, fl_stats* out) {
+    if (!h || !out) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    DevStats ds;
+    FL_CUDA(h, cudaMemcpyAsync(&ds, h->dst, sizeof(ds), cudaMemcpyDeviceToHost, h->stream));
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    std::memset(out, 0, sizeof(*out));
+    out->liquid_cells = ds.liquid;
+    out->cg_iterations = ds.cg_iters;
+    out->stray_particles = ds.strays;
+    out->device_status = ds.status;
+    out->substeps = h->substeps;
+    out->rs_initial = ds.rs_init;
+    out->rs_final = ds.rs_final;
+    return FL_OK;
+}
+
+// State blob: header, particles (n*32 B), ids (n*4 B), pressure (C*4 B).
+struct StateHeader {
+    char magic[8];
+    uint32_t version, nx, ny, nz, n, pad;
+    uint64_t substeps;
+};
+
+fl_status fl_save_state(fl_handle* h, void* buf, size_t* size_inout) {
+    if (!h || !size_inout) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    const size_t need = sizeof(StateHeader) + (size_t)h->n * 36 + 4 * (size_t)h->C;
+    if (!buf) {
+        *size_inout = need;
+        return FL_OK;
+    }
+    if (*size_inout < need) return set_err(h, FL_INVALID_ARG, "buffer too small");
+    StateHeader hd{};
+    std::memcpy(hd.magic, "FLGBSTAT", 8);
+    hd.version = 1; hd.nx = h->nx; hd.ny = h->ny; hd.nz = h->nz; hd.n = h->n; hd.substeps = h->substeps;
+    char* p = (char*)buf;
+    std::memcpy(p, &hd, sizeof(hd));
+    p += sizeof(hd);
+    if (h->n) {
+        FL_CUDA(h, cudaMemcpyAsync(p, h->partA, (size_t)h->n * 32, cudaMemcpyDeviceToHost, h->stream));
+        p += (size_t)h->n * 32;
+        FL_CUDA(h, cudaMemcpyAsync(p, h->idsA, (size_t)h->n * 4, cudaMemcpyDeviceToHost, h->stream));
+        p += (size_t)h->n * 4;
+    }
+    FL_CUDA(h, cudaMemcpyAsync(p, h->b.p, 4 * (size_t)h->C, cudaMemcpyDeviceToHost, h->stream));
+    *size_inout = need;
+    return read_status(h);
+}
+
+fl_status fl_load_state(fl_handle* h, const void* buf, size_t size) {
+    if (!h || !buf) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    if (size < sizeof(StateHeader)) return set_err(h, FL_INVALID_ARG, "state blob too small");
+    StateHeader hd;
+    std::memcpy(&hd, buf, sizeof(hd));
+    if (std::memcmp(hd.magic, "FLGBSTAT", 8) != 0 || hd.version != 1)
+        return set_err(h, FL_INVALID_ARG, "not a state blob of this library");
+    if (hd.nx != h->nx || hd.ny != h->ny || hd.nz != h->nz) return set_err(h, FL_INVALID_ARG, "grid mismatch");
+    if (hd.n > h->cap) return set_err(h, FL_INVALID_ARG, "particle count exceeds capacity");
+    const size_t need = sizeof(StateHeader) + (size_t)hd.n * 36 + 4 * (size_t)h->C;
+    if (size < need) return set_err(h, FL_INVALID_ARG, "state blob truncated");
+    const char* p = (const char*)buf + sizeof(hd);
+    h->n = hd.n;
+    if (h->n) {
+        FL_CUDA(h, cudaMemcpyAsync(h->partA, p, (size_t)h->n * 32, cudaMemcpyHostToDevice, h->stream));
+        p += (size_t)h->n * 32;
+        FL_CUDA(h, cudaMemcpyAsync(h->idsA, p, (size_t)h->n * 4, cudaMemcpyHostToDevice, h->stream));
+        p += (size_t)h->n * 4;
+    }
+    FL_CUDA(h, cudaMemcpyAsync(h->b.p, p, 4 * (size_t)h->C, cudaMemcpyHostToDevice, h->stream));
+    h->substeps = hd.substeps;
+    fl_status s = upload_params(h);
+    if (s != FL_OK) return s;
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return FL_OK;
+}
+
+fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type, const float* divergence,
+                            const float* pressure_in, float* pressure_out, float h, float rho, float dt,
+                            uint32_t max_iters, uint32_t warm_start, float tolerance, uint32_t cg_precision,
+                            fl_stats* stats_out) {
+    if (!cell_type || !divergence || !pressure_out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    if (warm_start && !pressure_in) return set_err(nullptr, FL_INVALID_ARG, "warm start needs pressure_in");
+    if (nx < 3 || ny < 3 || nz < 3 || (uint64_t)nx * ny * nz > (1ull << 30))
+        return set_err(nullptr, FL_INVALID_ARG, "bad grid size");
+    if (!(h > 0.0f) || !(rho > 0.0f) || !(dt > 0.0f)) return set_err(nullptr, FL_INVALID_ARG, "h, rho, dt must be > 0");
+    if (cg_precision > 1u) return set_err(nullptr, FL_INVALID_ARG, "bad cg_precision");
+    fl_status s = device_check(nullptr);
+    if (s != FL_OK) return s;
+    fl_params prm;
+    std::memset(&prm, 0, sizeof(prm));
+    prm.gdim[0] = nx; prm.gdim[1] = ny; prm.gdim[2] = nz;
+    prm.geom[0] = h; prm.geom[1] = 1.0f / h; prm.geom[2] = dt; prm.geom[3] = 65536.0f;
+    prm.phys[1] = rho;
+    prm.dims[2] = max_iters;
+    prm.dims[3] = warm_start ? 1u : 0u;
+    prm.pressure_tolerance = tolerance;
+    prm.cg_precision = cg_precision;
+    DevParams hp;
+    derive(prm, 0, hp);
+    const size_t C = hp.C;
+    const uint32_t nchunks = hp.nchunks;
+    fl::LaunchCfg L = make_cfg(nchunks);
+    PoolPlan pl;
+    size_t o_ct = pl.take<uint8_t>(C), o_div = pl.take<float>(C), o_p = pl.take<float>(C), o_r = pl.take<float>(C),
+           o_dA = pl.take<float>(C), o_dB = pl.take<float>(C), o_q = pl.take<float>(C);
+    size_t o_flag = pl.take<uint8_t>(nchunks), o_prr = pl.take<float>(nchunks), o_pdq = pl.take<float>(nchunks);
+    size_t o_c64 = pl.take<double>(nchunks), o_cta = pl.take<double>(2 * (size_t)L.cg_blocks);
+    size_t o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
+    void* pool = nullptr;
+    cudaError_t e = cudaMalloc(&pool, pl.off);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return set_err(nullptr, FL_OOM, "cudaMalloc failed");
+    }
+    char* base = (char*)pool;
+    DevBufs b{};
+    b.prm = (DevParams*)(base + o_prm);
+    b.st = (DevStats*)(base + o_st);
+    b.ct = (uint8_t*)(base + o_ct);
+    b.p = (float*)(base + o_p);
+    b.r = (float*)(base + o_r);
+    b.dA = (float*)(base + o_dA);
+    b.dB = (float*)(base + o_dB);
+    b.q = (float*)(base + o_q);
+    b.chunk_flag = (uint8_t*)(base + o_flag);
+    b.part_rr = (float*)(base + o_prr);
+    b.part_dq = (float*)(base + o_pdq);
+    b.chunk_rr64 = (double*)(base + o_c64);
+    b.cta_part64 = (double*)(base + o_cta);
+    float* ddiv = (float*)(base + o_div);
+    cudaStream_t st = nullptr;
+    fl_status rs = FL_OK;
+    DevStats ds{};
+    do {
+        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(pool, 0, pl.off, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync((void*)b.prm, &hp, sizeof(hp), cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(b.ct, cell_type, C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ddiv, divergence, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+        if (warm_start && (e = cudaMemcpyAsync(b.p, pressure_in, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+        if ((e = fl::launch_solve_init(b, (uint32_t)C, ddiv, st)) != cudaSuccess) break;
+        if ((e = fl::launch_cg(b, L, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(pressure_out, b.p, 4 * C, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(&ds, b.st, sizeof(ds), cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+        e = cudaStreamSynchronize(st);
+    } while (0);
+    if (e != cudaSuccess) rs = cuda_err(nullptr, e, "fl_solve_pressure");
+    if (st) cudaStreamDestroy(st);
+    cudaFree(pool);
+    if (rs != FL_OK) return rs;
+    if (ds.status) return set_err(nullptr, (fl_status)ds.status, "a device-side wait expired");
+    if (stats_out) {
+        std::memset(stats_out, 0, sizeof(*stats_out));
+        stats_out->cg_iterations = ds.cg_iters;
+        stats_out->rs_initial = ds.rs_init;
+        stats_out->rs_final = ds.rs_final;
+    }
+    return FL_OK;
+}
+
+const char* fl_last_error(const fl_handle* h) {
+    if (h) return h->err.c_str();
+    return g_err.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,314 @@
+"""ctypes binding of libfluidgb (include/fluidgb.h).
+
+`Fluid` mirrors the reference's `GpuFluid` life cycle (gpu/fluid.rs): create
+from a settings block, upload particles, step, live-update settings, impulse,
+reset, and read back particles / grid / bins / stats.  Every call goes through
+the C ABI; there is no Python or CPU fallback — if the shared library is
+missing the import of the binding fails loudly.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libfluidgb.so")
+
+FL_OK, FL_INVALID_ARG, FL_OOM, FL_CUDA_ERROR, FL_NOT_CONVERGED, FL_TIMEOUT, FL_NO_DEVICE, FL_INTERNAL = range(8)
+FL_CELL_SOLID, FL_CELL_LIQUID, FL_CELL_AIR = 0, 1, 2
+FL_CG_F32, FL_CG_F64 = 0, 1
+
+c_u32 = ctypes.c_uint32
+c_f32 = ctypes.c_float
+
+
+class FlParams(ctypes.Structure):
+    """The reference's 128-byte Params (gpu/fluid.rs:25-39) + 32-byte extension."""
+    _fields_ = [
+        ("dims", c_u32 * 4), ("geom", c_f32 * 4), ("phys", c_f32 * 4), ("origin", c_f32 * 4),
+        ("grav", c_f32 * 4), ("spc", c_f32 * 4), ("cls", c_f32 * 4), ("gdim", c_u32 * 4),
+        ("pressure_tolerance", c_f32), ("cg_precision", c_u32), ("advect_order", c_u32),
+        ("sort_period", c_u32), ("reserved", c_u32 * 4),
+    ]
+
+    def copy(self):
+        p = FlParams()
+        ctypes.memmove(ctypes.byref(p), ctypes.byref(self), ctypes.sizeof(FlParams))
+        return p
+
+    @property
+    def grid(self):
+        return tuple(int(x) for x in self.gdim[:3])
+
+
+class FlStats(ctypes.Structure):
+    _fields_ = [
+        ("liquid_cells", c_u32), ("cg_iterations", c_u32), ("stray_particles", c_u32),
+        ("device_status", c_u32), ("substeps", ctypes.c_uint64), ("rs_initial", ctypes.c_double),
+        ("rs_final", ctypes.c_double),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class FlGridView(ctypes.Structure):
+    _fields_ = [
+        ("u", _fp), ("v", _fp), ("w", _fp), ("u_saved", _fp), ("v_saved", _fp), ("w_saved", _fp),
+        ("pressure", _fp), ("cell_type", ctypes.POINTER(ctypes.c_uint8)),
+        ("counts", ctypes.POINTER(c_u32)), ("offsets", ctypes.POINTER(c_u32)),
+    ]
+
+
+assert ctypes.sizeof(FlParams) == 160
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "fl_abi_version": (c_u32, []),
+    "fl_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "fl_params_default": (ctypes.c_int, [ctypes.POINTER(FlParams), c_u32, c_u32, c_u32, c_f32, _fp]),
+    "fl_create": (ctypes.c_int, [ctypes.POINTER(FlParams), c_u32, ctypes.POINTER(ctypes.c_void_p)]),
+    "fl_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_set_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlParams)]),
+    "fl_get_params": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlParams)]),
+    "fl_set_particles": (ctypes.c_int, [ctypes.c_void_p, _fp, c_u32]),
+    "fl_get_particles": (ctypes.c_int, [ctypes.c_void_p, _fp, ctypes.POINTER(c_u32)]),
+    "fl_particle_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32)]),
+    "fl_step": (ctypes.c_int, [ctypes.c_void_p, c_u32]),
+    "fl_step_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32]),
+    "fl_step_host": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, c_u32, c_u32]),
+    "fl_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fl_get_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.POINTER(ctypes.c_uint64)]),
+    "fl_reset_stage_times": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_apply_impulse": (ctypes.c_int, [ctypes.c_void_p, _fp]),
+    "fl_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_get_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlGridView)]),
+    "fl_get_bins": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32), ctypes.POINTER(c_u32),
+                                   ctypes.POINTER(c_u32)]),
+    "fl_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlStats)]),
+    "fl_save_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "fl_load_state": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "fl_solve_pressure": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.POINTER(ctypes.c_uint8), _fp, _fp, _fp,
+                                         c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
+                                         ctypes.POINTER(FlStats)]),
+    "fl_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+}
+
+# FL_STAGE_* order (include/fluidgb.h)
+STAGES = ("sort", "classify", "scatter", "prep", "cg", "gradient", "g2p")
+
+_lib = None
+
+
+def load_library(path=None):
+    """Load libfluidgb.so (built by fluidgb.build).  Raises if it is missing."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("libfluidgb.so not found at %s: run fluidgb.build.build() (needs nvcc)" % p)
+    lib = ctypes.CDLL(p)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.fl_abi_version() != 1:
+        raise RuntimeError("libfluidgb ABI version mismatch")
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class FluidError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_STATUS.get(status, status), msg))
+        self.status = status
+
+
+_STATUS = {0: "FL_OK", 1: "FL_INVALID_ARG", 2: "FL_OOM", 3: "FL_CUDA_ERROR", 4: "FL_NOT_CONVERGED",
+           5: "FL_TIMEOUT", 6: "FL_NO_DEVICE", 7: "FL_INTERNAL"}
+
+
+def _check(lib, status, handle=None):
+    if status != FL_OK:
+        msg = lib.fl_last_error(handle)
+        raise FluidError(status, msg.decode() if msg else "")
+
+
+def _f32p(a):
+    return a.ctypes.data_as(_fp)
+
+
+def _u32p(a):
+    return a.ctypes.data_as(ctypes.POINTER(c_u32))
+
+
+def default_params(nx, ny, nz, h, origin=None):
+    """Registry defaults (settings/mod.rs) for an nx*ny*nz tank of cell size h."""
+    lib = load_library()
+    p = FlParams()
+    o = None if origin is None else (ctypes.c_float * 3)(*origin)
+    _check(lib, lib.fl_params_default(ctypes.byref(p), nx, ny, nz, h, o))
+    return p
+
+
+def face_counts(nx, ny, nz):
+    return ((nx + 1) * ny * nz, nx * (ny + 1) * nz, nx * ny * (nz + 1))
+
+
+class Fluid:
+    """One simulation handle on the current CUDA device."""
+
+    def __init__(self, params, capacity, lib=None):
+        self.lib = lib or load_library()
+        self.params = params.copy()
+        self.capacity = int(capacity)
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.fl_create(ctypes.byref(self.params), self.capacity, ctypes.byref(h)))
+        self.h = h
+        nx, ny, nz = params.grid
+        self.dims = (nx, ny, nz)
+        self.C = nx * ny * nz
+        self.F = face_counts(nx, ny, nz)
+
+    def close(self):
+        if self.h:
+            self.lib.fl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _c(self, status):
+        _check(self.lib, status, self.h)
+
+    def set_params(self, params):
+        self._c(self.lib.fl_set_params(self.h, ctypes.byref(params)))
+        self.params = params.copy()
+
+    def set_particles(self, parts):
+        a = np.ascontiguousarray(parts, dtype=np.float32).reshape(-1, 8)
+        self._c(self.lib.fl_set_particles(self.h, _f32p(a), a.shape[0]))
+
+    def particle_count(self):
+        n = c_u32()
+        self._c(self.lib.fl_particle_count(self.h, ctypes.byref(n)))
+        return n.value
+
+    def get_particles(self, with_ids=True):
+        n = self.particle_count()
+        out = np.empty((n, 8), np.float32)
+        ids = np.empty(n, np.uint32) if with_ids else None
+        self._c(self.lib.fl_get_particles(self.h, _f32p(out), _u32p(ids) if with_ids else None))
+        return (out, ids) if with_ids else out
+
+    def step(self, substeps=1):
+        self._c(self.lib.fl_step(self.h, substeps))
+
+    def step_device(self, ptr, n):
+        self._c(self.lib.fl_step_device(self.h, ctypes.c_void_p(ptr), n))
+
+    def step_host(self, parts_in, parts_out, substeps=1):
+        """Host buffers in/out (fl_step_host); arrays are (n, 8) float32."""
+        n = parts_in.shape[0]
+        self._c(self.lib.fl_step_host(self.h, _f32p(parts_in), _f32p(parts_out), n, substeps))
+
+    def set_profiling(self, on=True):
+        self._c(self.lib.fl_set_profiling(self.h, 1 if on else 0))
+
+    def stage_times(self):
+        """({stage: ms total}, substeps timed)."""
+        ms = (ctypes.c_double * len(STAGES))()
+        n = ctypes.c_uint64()
+        self._c(self.lib.fl_get_stage_times(self.h, ms, ctypes.byref(n)))
+        return {k: ms[i] for i, k in enumerate(STAGES)}, n.value
+
+    def reset_stage_times(self):
+        self._c(self.lib.fl_reset_stage_times(self.h))
+
+    def sync(self):
+        self._c(self.lib.fl_sync(self.h))
+
+    def set_stream(self, stream_ptr):
+        self._c(self.lib.fl_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def apply_impulse(self, dv):
+        v = (ctypes.c_float * 3)(*dv)
+        self._c(self.lib.fl_apply_impulse(self.h, v))
+
+    def reset(self):
+        self._c(self.lib.fl_reset(self.h))
+
+    def get_grid(self):
+        fu, fv, fw = self.F
+        g = {
+            "u": np.empty(fu, np.float32), "v": np.empty(fv, np.float32), "w": np.empty(fw, np.float32),
+            "u_saved": np.empty(fu, np.float32), "v_saved": np.empty(fv, np.float32),
+            "w_saved": np.empty(fw, np.float32), "pressure": np.empty(self.C, np.float32),
+            "cell_type": np.empty(self.C, np.uint8), "counts": np.empty(self.C, np.uint32),
+            "offsets": np.empty(self.C, np.uint32),
+        }
+        v = FlGridView()
+        for k in ("u", "v", "w", "u_saved", "v_saved", "w_saved", "pressure"):
+            setattr(v, k, _f32p(g[k]))
+        v.cell_type = g["cell_type"].ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+        v.counts = _u32p(g["counts"])
+        v.offsets = _u32p(g["offsets"])
+        self._c(self.lib.fl_get_grid(self.h, ctypes.byref(v)))
+        return g
+
+    def get_bins(self):
+        n = self.particle_count()
+        counts = np.empty(self.C, np.uint32)
+        offsets = np.empty(self.C, np.uint32)
+        perm = np.empty(n, np.uint32)
+        self._c(self.lib.fl_get_bins(self.h, _u32p(counts), _u32p(offsets), _u32p(perm)))
+        return counts, offsets, perm
+
+    def stats(self):
+        s = FlStats()
+        self._c(self.lib.fl_get_stats(self.h, ctypes.byref(s)))
+        return s.as_dict()
+
+    def save_state(self):
+        size = ctypes.c_size_t(0)
+        self._c(self.lib.fl_save_state(self.h, None, ctypes.byref(size)))
+        buf = ctypes.create_string_buffer(size.value)
+        self._c(self.lib.fl_save_state(self.h, buf, ctypes.byref(size)))
+        return bytes(buf.raw[: size.value])
+
+    def load_state(self, blob):
+        buf = ctypes.create_string_buffer(blob, len(blob))
+        self._c(self.lib.fl_load_state(self.h, buf, len(blob)))
+
+
+def solve_pressure(cell_type, div, dims, h, rho, dt, max_iters, warm_start=False, pressure_in=None,
+                   tolerance=0.0, precision=FL_CG_F32, lib=None):
+    """GPU CG on host arrays (fl_solve_pressure).  Returns (pressure, stats)."""
+    lib = lib or load_library()
+    nx, ny, nz = dims
+    ct = np.ascontiguousarray(cell_type, dtype=np.uint8)
+    dv = np.ascontiguousarray(div, dtype=np.float32)
+    pin = np.ascontiguousarray(pressure_in if pressure_in is not None else np.zeros_like(dv), dtype=np.float32)
+    pout = np.empty_like(dv)
+    st = FlStats()
+    _check(lib, lib.fl_solve_pressure(nx, ny, nz, ct.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _f32p(dv),
+                                      _f32p(pin), _f32p(pout), h, rho, dt, max_iters, 1 if warm_start else 0,
+                                      tolerance, precision, ctypes.byref(st)))
+    return pout, st.as_dict()

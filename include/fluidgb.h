@@ -1,0 +1,212 @@
+/*
+ * fluidgb.h — C ABI of the GB300-native (sm_103a) FLIP/PIC substep.
+ *
+ * The library replaces the per-substep compute passes of fluid-lab's
+ * `GpuFluid` (app/crates/fluid-lab/src/gpu/fluid.rs) behind plain C types:
+ * particle buffers in, particle buffers out, and the same 128-byte `Params`
+ * settings block.  All functions return an `fl_status`; none aborts and no
+ * kernel traps.  A handle is not thread-safe; different handles may be used
+ * from different threads.  Work is enqueued on the handle's CUDA stream and is
+ * asynchronous until `fl_sync` or a call that copies to host memory.
+ *
+ * Reference interfaces replaced (file:line within the reference project):
+ *   GpuFluid::new / GpuContext::recreate_fluid  app/crates/fluid-lab/src/gpu/fluid.rs:247-318,
+ *                                               app/crates/fluid-lab/src/gpu/mod.rs:500-625
+ *   GpuContext::step(substeps)                  app/crates/fluid-lab/src/gpu/mod.rs:950-989
+ *   record_prep_pre_sort / record_sort /
+ *   record_prep_post_sort / record_pressure /
+ *   record_finish                               app/crates/fluid-lab/src/gpu/fluid.rs:1436-1715
+ *   live setters (set_flip_blend ...)           app/crates/fluid-lab/src/gpu/fluid.rs:1294-1371
+ *   apply_impulse                               app/crates/fluid-lab/src/gpu/fluid.rs:1374-1395
+ *   reset                                       app/crates/fluid-lab/src/gpu/fluid.rs:1408-1418
+ *   particle_buffer()                           app/crates/fluid-lab/src/gpu/fluid.rs:1208-1214
+ */
+#ifndef FLUIDGB_H
+#define FLUIDGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FL_ABI_VERSION 1u
+
+typedef enum fl_status {
+    FL_OK = 0,
+    FL_INVALID_ARG = 1,   /* bad pointer, size, or parameter; nothing was enqueued */
+    FL_OOM = 2,           /* device or host allocation failed */
+    FL_CUDA_ERROR = 3,    /* a CUDA runtime call failed; see fl_last_error */
+    FL_NOT_CONVERGED = 4, /* reserved: CG stopped at the iteration cap (informational) */
+    FL_TIMEOUT = 5,       /* a bounded device-side wait expired; the context stays usable */
+    FL_NO_DEVICE = 6,     /* no CUDA device, or it is not an sm_103 part */
+    FL_INTERNAL = 7
+} fl_status;
+
+/* Cell classification, same numbering as the reference's `CellType`
+ * (app/crates/fluid-lab/src/sim/mod.rs:30-36). */
+enum { FL_CELL_SOLID = 0, FL_CELL_LIQUID = 1, FL_CELL_AIR = 2 };
+
+/* CG inner-product precision (extension field `cg_precision`). */
+enum {
+    FL_CG_F32 = 0, /* reference arithmetic: f32 two-level 256-wide tree dots (cg_reduce.wgsl) */
+    FL_CG_F64 = 1  /* f64 inner products, residual norm and convergence test */
+};
+
+/*
+ * fl_params — the reference's 128-byte `Params` uniform
+ * (app/crates/fluid-lab/src/gpu/fluid.rs:25-39, filled at :289-318), field for
+ * field, followed by a 32-byte extension block.  A caller holding the
+ * reference's `Params` bytes can copy them into the first 128 bytes.
+ */
+typedef struct fl_params {
+    uint32_t dims[4];   /* nx (legacy, ignored), particle_count (ignored: set by
+                           fl_set_particles), pressure_iters (0 -> 1), warm_start */
+    float geom[4];      /* h, inv_h, dt, fixed_scale (2^16) */
+    float phys[4];      /* gravity_y (legacy, ignored), rho, flip_blend, wall_friction */
+    float origin[4];    /* world position of cell (0,0,0)'s min corner; w ignored */
+    float grav[4];      /* gx, gy, gz, _ */
+    float spc[4];       /* rest_per_cell, volume_stiffness, drift_clamp, _ */
+    float cls[4];       /* liquid_threshold, surface_dilation, cfl, _ */
+    uint32_t gdim[4];   /* nx, ny, nz, 0 */
+    /* ---- extension block (not part of the reference's Params) ---- */
+    float pressure_tolerance; /* relative residual tolerance; 0 = off; clamped to
+                                 [0, 0.1] like set_pressure_residual_tolerance
+                                 (fluid.rs:47-50, :1362-1369) */
+    uint32_t cg_precision;    /* FL_CG_F32 or FL_CG_F64 */
+    uint32_t advect_order;    /* 1 = forward Euler (reference g2p.wgsl:186); 2 = midpoint */
+    uint32_t sort_period;     /* accepted for drop-in compatibility; the layout is
+                                 re-sorted every substep (the gather-form P2G reads bins) */
+    uint32_t reserved[4];     /* must be zero */
+} fl_params;
+
+typedef struct fl_handle fl_handle;
+
+/* Statistics of the most recent substep. */
+typedef struct fl_stats {
+    uint32_t liquid_cells;    /* stats[0] of classify.wgsl */
+    uint32_t cg_iterations;   /* iterations that ran with `active` set */
+    uint32_t stray_particles; /* particles whose P2G base differs from their bin (ulp ties) */
+    uint32_t device_status;   /* 0, or the fl_status a kernel recorded */
+    uint64_t substeps;        /* substeps run since fl_create / fl_reset */
+    double rs_initial;        /* r.r after CG init */
+    double rs_final;          /* r.r at exit */
+} fl_stats;
+
+/* Host destinations for fl_get_grid; any NULL member is skipped. */
+typedef struct fl_grid_view {
+    float* u;        /* (nx+1)*ny*nz, final (post-projection) face velocity */
+    float* v;        /* nx*(ny+1)*nz */
+    float* w;        /* nx*ny*(nz+1) */
+    float* u_saved;  /* post-P2G, pre-force snapshot used by the FLIP delta */
+    float* v_saved;
+    float* w_saved;
+    float* pressure; /* nx*ny*nz */
+    uint8_t* cell_type; /* nx*ny*nz, FL_CELL_* */
+    uint32_t* counts;   /* nx*ny*nz particle histogram (occupancy) */
+    uint32_t* offsets;  /* nx*ny*nz exclusive prefix sum of counts */
+} fl_grid_view;
+
+/* Version of this ABI (FL_ABI_VERSION of the library that was loaded). */
+uint32_t fl_abi_version(void);
+const char* fl_status_string(fl_status s);
+
+/* Fill `out` with the reference registry defaults (settings/mod.rs:498-724) for a
+ * tank of nx*ny*nz cells of size h whose min corner is `origin` (NULL = centred
+ * like fluid.rs:262-269).  Replaces the Params construction at fluid.rs:289-318. */
+fl_status fl_params_default(fl_params* out, uint32_t nx, uint32_t ny, uint32_t nz, float h,
+                            const float* origin);
+
+/* Allocate device state for a grid and at most `capacity` particles.
+ * Replaces GpuFluid::new (fluid.rs:247-1197). */
+fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out);
+fl_status fl_destroy(fl_handle* h);
+
+/* Live parameter update (fluid.rs:1294-1371).  Grid dimensions cannot change:
+ * INVALID_ARG (create a new handle instead, like GpuContext::recreate_fluid). */
+fl_status fl_set_params(fl_handle* h, const fl_params* params);
+fl_status fl_get_params(const fl_handle* h, fl_params* out);
+
+/* Upload n particles as 8 floats each {pos.xyz, _, vel.xyz, _} (fluid.rs:116-123);
+ * they also become the state fl_reset restores.  Particle ids are 0..n-1. */
+fl_status fl_set_particles(fl_handle* h, const float* pos_vel_aos32, uint32_t n);
+/* Download the current particles (8 floats each) and, if ids_out != NULL, the
+ * id of the particle in each slot. */
+fl_status fl_get_particles(fl_handle* h, float* pos_vel_aos32_out, uint32_t* ids_out);
+fl_status fl_particle_count(const fl_handle* h, uint32_t* n_out);
+
+/* Run `substeps` fixed-dt substeps on the handle's particles (GpuContext::step). */
+fl_status fl_step(fl_handle* h, uint32_t substeps);
+/* One substep on a caller-owned device buffer of n particles (8 floats each,
+ * 16-byte aligned).  The buffer is read, and on return holds the advanced
+ * particles in this substep's bin order.  n <= capacity. */
+fl_status fl_step_device(fl_handle* h, void* particles_dev, uint32_t n);
+
+/* Host-memory variant: copy n particles from `in` (pinned memory overlaps best)
+ * into the handle, run `substeps`, copy the result to `out` (may equal `in`),
+ * and wait.  The handle keeps the advanced particles and its warm-start
+ * pressure; particle ids are not maintained by this call.  n <= capacity. */
+fl_status fl_step_host(fl_handle* h, const float* in, float* out, uint32_t n, uint32_t substeps);
+
+fl_status fl_sync(fl_handle* h);
+/* Use a caller stream (cudaStream_t passed as void*; NULL = the handle's own). */
+fl_status fl_set_stream(fl_handle* h, void* cuda_stream);
+
+/* Add dv to every particle velocity (impulse.wgsl; fluid.rs:1374-1395). */
+fl_status fl_apply_impulse(fl_handle* h, const float dv[3]);
+/* Restore the particles of the last fl_set_particles and zero the pressure
+ * (fluid.rs:1408-1418). */
+fl_status fl_reset(fl_handle* h);
+
+/* Copy grid state of the last substep to host memory. */
+fl_status fl_get_grid(fl_handle* h, const fl_grid_view* view);
+/* Bins of the last substep's counting sort: per-cell counts and exclusive
+ * offsets, and perm[d] = pre-sort slot of the particle placed in slot d.  The
+ * permutation is stable (lib.rs:1188-1211).  Any pointer may be NULL. */
+fl_status fl_get_bins(fl_handle* h, uint32_t* counts, uint32_t* offsets, uint32_t* perm);
+fl_status fl_get_stats(fl_handle* h, fl_stats* out);
+
+/* Checkpoint: particles, ids, warm-start pressure and step counter.  Call with
+ * buf == NULL to learn the size.  Resume is bit-exact. */
+fl_status fl_save_state(fl_handle* h, void* buf, size_t* size_inout);
+fl_status fl_load_state(fl_handle* h, const void* buf, size_t size);
+
+/* Per-stage device time, measured with CUDA events on the handle's stream
+ * (the sections of the reference's GpuTimers, gpu/timing.rs:32-59, grouped by
+ * kernel).  While profiling is on, fl_step launches stage by stage and waits at
+ * the end of every substep; totals accumulate until fl_reset_stage_times. */
+enum {
+    FL_STAGE_SORT = 0,      /* mark + counting sort (histogram, scan, stable scatter, gather) */
+    FL_STAGE_CLASSIFY = 1,  /* classify */
+    FL_STAGE_SCATTER = 2,   /* P2G */
+    FL_STAGE_PREP = 3,      /* normalize, save_vel, forces, bound_pre, divergence, cg_init */
+    FL_STAGE_CG = 4,        /* the CG iterations */
+    FL_STAGE_GRADIENT = 5,  /* gradient (+ bound_post) */
+    FL_STAGE_G2P = 6,       /* g2p */
+    FL_STAGE_COUNT = 7
+};
+fl_status fl_set_profiling(fl_handle* h, int enable);
+/* ms_out[FL_STAGE_COUNT]: summed milliseconds; substeps_out: substeps timed. */
+fl_status fl_get_stage_times(fl_handle* h, double* ms_out, uint64_t* substeps_out);
+fl_status fl_reset_stage_times(fl_handle* h);
+
+/* Stand-alone pressure solve on host arrays: the MAC-Poisson CG of
+ * cg_init/cg_spmv/.../cg_dir.wgsl with the step's semantics, for cell types
+ * (FL_CELL_*), a divergence field and an initial pressure (used only when
+ * warm_start != 0).  Replaces sim/pressure.rs cg_solve_with_options
+ * (app/crates/fluid-lab/src/sim/pressure.rs:235-309) on the GPU.
+ * rhs = -(rho*h*h/dt)*div.  Writes pressure_out and, if non-NULL, stats. */
+fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type,
+                            const float* divergence, const float* pressure_in, float* pressure_out,
+                            float h, float rho, float dt, uint32_t max_iters, uint32_t warm_start,
+                            float tolerance, uint32_t cg_precision, fl_stats* stats_out);
+
+/* Message of the last failing call on `h` (or of the last failing fl_create /
+ * fl_solve_pressure when h == NULL).  Never NULL. */
+const char* fl_last_error(const fl_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUIDGB_H */

@@ -1,0 +1,91 @@
+"""The C ABI library on the CPU host: it loads, exports every symbol the header
+declares, has the reference's Params layout, and fails cleanly without a GPU.
+No compute call is made here."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fluidgb import FlParams, FlStats, SIGNATURES, scenes
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(REPO, "include", "fluidgb.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(fl_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_header_declares_the_step_api():
+    names = declared_functions()
+    for required in ("fl_create", "fl_destroy", "fl_set_params", "fl_set_particles", "fl_get_particles",
+                     "fl_step", "fl_step_device", "fl_apply_impulse", "fl_reset", "fl_get_grid", "fl_get_bins",
+                     "fl_get_stats", "fl_save_state", "fl_load_state", "fl_last_error", "fl_solve_pressure"):
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol(fluidlib):
+    for name in declared_functions():
+        assert hasattr(fluidlib, name), name
+    assert set(declared_functions()) == set(SIGNATURES), "ctypes binding and header disagree"
+
+
+def test_abi_version(fluidlib):
+    assert fluidlib.fl_abi_version() == 1
+
+
+def test_params_layout_is_the_reference_uniform():
+    # gpu/fluid.rs:25-39: 8 x vec4 = 128 bytes, then the extension block
+    offs = {name: getattr(FlParams, name).offset for name, _ in FlParams._fields_}
+    assert [offs[k] for k in ("dims", "geom", "phys", "origin", "grav", "spc", "cls", "gdim")] == \
+        [0, 16, 32, 48, 64, 80, 96, 112]
+    assert offs["pressure_tolerance"] == 128
+    assert ctypes.sizeof(FlParams) == 160
+    assert ctypes.sizeof(FlStats) == 40
+
+
+def test_params_default_is_the_registry(fluidlib):
+    p = FlParams()
+    assert fluidlib.fl_params_default(ctypes.byref(p), 80, 40, 80, 2.0 / 64.0, None) == 0
+    assert list(p.gdim[:3]) == [80, 40, 80]
+    assert list(p.dims) == [80, 0, 30, 1]
+    assert p.geom[2] == np.float32(1.0 / 120.0) and p.geom[3] == 65536.0
+    assert p.phys[1] == 1000.0 and p.phys[2] == np.float32(0.9)
+    assert p.origin[0] == np.float32(-80 * (2.0 / 64.0) / 2.0)
+    assert p.cls[2] == 2.0 and p.spc[1] == np.float32(0.45)
+    # the Python scene builder fills the same fields
+    q = scenes.params_for(32, flip=0.9, iters=30, tol=0.0)
+    r = FlParams()
+    fluidlib.fl_params_default(ctypes.byref(r), 32, 32, 32, 1.0 / 32, (ctypes.c_float * 3)(0, 0, 0))
+    for f in ("geom", "phys", "grav", "spc", "cls", "gdim"):
+        assert list(getattr(q, f)) == list(getattr(r, f)), f
+
+
+def test_invalid_arguments_are_rejected_without_a_device(fluidlib):
+    h = ctypes.c_void_p()
+    assert fluidlib.fl_create(None, 10, ctypes.byref(h)) == 1
+    assert b"NULL" in fluidlib.fl_last_error(None)
+    p = scenes.params_for(2)            # < 3 cells per axis
+    assert fluidlib.fl_create(ctypes.byref(p), 10, ctypes.byref(h)) == 1
+    p = scenes.params_for(16)
+    p.reserved[0] = 7
+    assert fluidlib.fl_create(ctypes.byref(p), 10, ctypes.byref(h)) == 1
+    assert fluidlib.fl_step(None, 1) == 1
+    assert fluidlib.fl_status_string(5) == b"FL_TIMEOUT"
+
+
+def test_create_without_gpu_reports_no_device(fluidlib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except ImportError:
+        pass
+    p = scenes.params_for(16)
+    h = ctypes.c_void_p()
+    assert fluidlib.fl_create(ctypes.byref(p), 10, ctypes.byref(h)) == 6  # FL_NO_DEVICE
+    assert not h.value

@@ -130,9 +130,20 @@ def test_non_power_of_two_cell_size_and_strays(lib, oracle):
     p = scenes.params_for(n, iters=60, tol=1e-4)
     parts = scenes.seed_particles(n, scenes.box(0.6, 0.5, 0.7), seed=7)
     h = np.float32(1.0) / np.float32(n)
-    k = np.arange(parts.shape[0]) % 7 == 0
-    parts[k, 0] = (np.round(parts[k, 0] / h) * h).astype(np.float32)
-    parts[k[::-1], 1] = (np.round(parts[k[::-1], 1] / h) * h).astype(np.float32)
+    inv_h = np.float32(1.0) / h
+    # coordinates one ulp below a cell face where x/h and x*inv_h floor differently
+    ties = []
+    for k in range(1, n - 1):
+        x = np.nextafter(np.float32(k) * h, np.float32(-1.0))
+        if np.floor(x / h) != np.floor(x * inv_h):
+            ties.append(x)
+    assert len(ties) >= 4
+    ties = np.array(ties, np.float32)
+    rng = np.random.default_rng(5)
+    for axis in (0, 1, 2):
+        sel = np.flatnonzero(rng.random(parts.shape[0]) < 0.1)
+        near = np.abs(ties[None, :] - parts[sel, axis][:, None]).argmin(axis=1)
+        parts[sel, axis] = ties[near]
     g, o = make_pair(oracle, p, parts)
     g.step(1)
     o.step(1)
@@ -267,9 +278,9 @@ def test_solve_pressure_matches_oracle_and_reference_thresholds(lib, oracle):
     l2 = _l2_after(oracle, d, ct, u, v, w, pg)
     assert l2 < 0.01 * l2_before and l2 <= _l2_after(oracle, d, ct, u, v, w, pj)
     # warm start and tolerance exit
-    pw, sw = _abi.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, warm_start=True, pressure_in=pg, tolerance=0.05)
+    pw, sw = _abi.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, warm_start=True, pressure_in=pg, tolerance=0.1)
     pwo, swo = oracle.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, warm_start=True, pressure_in=pg,
-                                     tolerance=0.05)
+                                     tolerance=0.1)
     assert np.array_equal(pw, pwo) and sw["cg_iterations"] == swo["cg_iterations"] < 40
     # f64 inner products
     p64, s64 = _abi.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, precision=FL_CG_F64)

@@ -55,6 +55,12 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_value(world, steps, ms_max):
+    """Whole-job steps/s of `world` independent replicas: all ranks' steps over
+    the slowest rank's time."""
+    return world * steps / (ms_max / 1000.0)
+
+
 def measured_peaks():
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -241,7 +247,7 @@ def run_ours(args):
     if world > 1:
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1000.0)
+    value = replica_value(world, args.steps, ms_max)
 
     # FP64-reduction variant on the same scene and schedule.
     fp64 = None

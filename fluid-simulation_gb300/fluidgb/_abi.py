@@ -97,6 +97,9 @@ SIGNATURES = {
     "fl_solve_pressure": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.POINTER(ctypes.c_uint8), _fp, _fp, _fp,
                                          c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
                                          ctypes.POINTER(FlStats)]),
+    "fl_solve_pressure_noalloc": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
+                                                 ctypes.c_void_p, c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
+                                                 ctypes.c_void_p, ctypes.POINTER(FlStats)]),
     "fl_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
 }
 

@@ -202,6 +202,26 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
                             float h, float rho, float dt, uint32_t max_iters, uint32_t warm_start,
                             float tolerance, uint32_t cg_precision, fl_stats* stats_out);
 
+/* Pressure solve that allocates nothing.  No counterpart in the reference:
+ * for callers that cannot call cudaMalloc around the solve (a frame loop with
+ * a no-allocation rule, a plugin whose host application owns every device
+ * allocation, a process that must not grow its device footprint after
+ * start-up).  Same solve and settings as fl_solve_pressure, but inputs and
+ * output are DEVICE pointers: cell types (u8), divergence, and pressure
+ * (read as the initial guess when warm_start != 0, overwritten with the
+ * result).  The CG scratch is one static device array sized for
+ * FL_NOALLOC_MAX_CELLS cells (about 4.1 MB, held by every GPU that loads the
+ * library until exit); larger grids return FL_INVALID_ARG.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress), so make
+ * it before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race.  Enqueues on `cuda_stream` (NULL = default stream) and
+ * waits for it; fills stats_out if non-NULL.  No error string is recorded. */
+#define FL_NOALLOC_MAX_CELLS 262144u
+fl_status fl_solve_pressure_noalloc(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type_dev,
+                                    const float* divergence_dev, float* pressure_dev, float h, float rho,
+                                    float dt, uint32_t max_iters, uint32_t warm_start, float tolerance,
+                                    uint32_t cg_precision, void* cuda_stream, fl_stats* stats_out);
+
 /* Message of the last failing call on `h` (or of the last failing fl_create /
  * fl_solve_pressure when h == NULL).  Never NULL. */
 const char* fl_last_error(const fl_handle* h);

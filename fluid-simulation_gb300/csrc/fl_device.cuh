@@ -74,6 +74,8 @@ struct DevBufs {
     uint32_t* spine;
     uint32_t* big_list;
     uint8_t* ct;
+    uint16_t* cinfo;       // per liquid cell: bit0 liquid, bits1-6 liquid neighbours (-x,+x,-y,+y,-z,+z),
+                           // bits 7-9 count of non-solid neighbours (cg_spmv.wgsl:46-66); 0 elsewhere
     uint8_t* chunk_flag;
     int32_t* num[3];
     int32_t* den[3];
@@ -84,6 +86,8 @@ struct DevBufs {
     float* part_dq;
     double* chunk_rr64;    // per-chunk f64 partials of the initial residual
     double* cta_part64;    // [2][max CTAs] f64 partials (FL_CG_F64)
+    uint32_t* cg_chunk;    // CG plan: active chunks grouped by (chunk mod 256), ascending
+    uint32_t* cg_off;      // CG plan: 257 segment offsets into cg_chunk
 };
 
 // ---------------------------------------------------------------------------

@@ -279,6 +279,19 @@ __device__ __forceinline__ float apply_A(const uint8_t* ct, const float* x, size
     return __fsub_rn(__fmul_rn(cnt, xc), sum);
 }
 
+// Stencil mask of a liquid (hence interior) cell, for the CG.
+__device__ __forceinline__ uint16_t stencil_info(const uint8_t* ct, size_t c, size_t nx, size_t nxy) {
+    const size_t nb[6] = {c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
+    uint32_t info = 1u, cnt = 0u;
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+        const uint8_t t = ct[nb[s]];
+        if (t != CELL_SOLID) cnt++;
+        if (t == CELL_LIQUID) info |= 2u << s;
+    }
+    return (uint16_t)(info | (cnt << 7));
+}
+
 __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
     __shared__ float s_tree[256];
     __shared__ double s_red[8];
@@ -323,12 +336,14 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
             const float rc = __fsub_rn(rhs, ap);
             b.r[c] = rc;
             b.dA[c] = rc;
+            b.cinfo[c] = stencil_info(b.ct, c, nx, (size_t)nx * ny);
             prod = __fmul_rn(rc, rc);
             prod64 = (double)rc * (double)rc;
         } else {
             b.p[c] = 0.0f;
             b.r[c] = 0.0f;
             b.dA[c] = 0.0f;
+            b.cinfo[c] = 0;
         }
     }
     const int any = __syncthreads_or(liquid);
@@ -400,12 +415,14 @@ __global__ void __launch_bounds__(256) k_solve_init(DevBufs b, uint32_t C, const
             const float rc = __fsub_rn(rhs, ap);
             b.r[c] = rc;
             b.dA[c] = rc;
+            b.cinfo[c] = stencil_info(b.ct, c, P.nx, (size_t)P.nx * P.ny);
             prod = __fmul_rn(rc, rc);
             prod64 = (double)rc * (double)rc;
         } else {
             b.p[c] = 0.0f;
             b.r[c] = 0.0f;
             b.dA[c] = 0.0f;
+            b.cinfo[c] = 0;
         }
     }
     const int any = __syncthreads_or(liquid);

@@ -325,7 +325,7 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     size_t o_scr = pl.take<uint32_t>(cap), o_stray = pl.take<uint32_t>(cap);
     size_t o_counts = pl.take<uint32_t>(C), o_offs = pl.take<uint32_t>(C), o_cur = pl.take<uint32_t>(C);
     size_t o_spine = pl.take<uint32_t>(nb), o_big = pl.take<uint32_t>(C);
-    size_t o_ct = pl.take<uint8_t>(C), o_flag = pl.take<uint8_t>(h->nchunks);
+    size_t o_ct = pl.take<uint8_t>(C), o_flag = pl.take<uint8_t>(h->nchunks), o_cinfo = pl.take<uint16_t>(C);
     size_t o_num[3], o_den[3], o_vel[3], o_sav[3];
     for (int a = 0; a < 3; a++) {
         o_num[a] = pl.take<int32_t>(h->F3[a]);
@@ -338,6 +338,7 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     size_t o_prr = pl.take<float>(h->nchunks), o_pdq = pl.take<float>(h->nchunks);
     size_t o_c64 = pl.take<double>(h->nchunks);
     size_t o_cta = pl.take<double>(2 * (size_t)g_num_sms * g_cg_per_sm);
+    size_t o_plan = pl.take<uint32_t>(h->nchunks), o_poff = pl.take<uint32_t>(fl::CHUNK + 1);
     size_t o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
     h->pool_bytes = pl.off;
 
@@ -380,6 +381,7 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     b.spine = (uint32_t*)(base + o_spine);
     b.big_list = (uint32_t*)(base + o_big);
     b.ct = (uint8_t*)(base + o_ct);
+    b.cinfo = (uint16_t*)(base + o_cinfo);
     b.chunk_flag = (uint8_t*)(base + o_flag);
     for (int a = 0; a < 3; a++) {
         b.num[a] = (int32_t*)(base + o_num[a]);
@@ -396,6 +398,8 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     b.part_dq = (float*)(base + o_pdq);
     b.chunk_rr64 = (double*)(base + o_c64);
     b.cta_part64 = (double*)(base + o_cta);
+    b.cg_chunk = (uint32_t*)(base + o_plan);
+    b.cg_off = (uint32_t*)(base + o_poff);
     if ((s = upload_params(h)) != FL_OK) {
         std::string m = h->err;
         fl_destroy(h);
@@ -719,7 +723,9 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     size_t o_ct = pl.take<uint8_t>(C), o_div = pl.take<float>(C), o_p = pl.take<float>(C), o_r = pl.take<float>(C),
            o_dA = pl.take<float>(C), o_dB = pl.take<float>(C), o_q = pl.take<float>(C);
     size_t o_flag = pl.take<uint8_t>(nchunks), o_prr = pl.take<float>(nchunks), o_pdq = pl.take<float>(nchunks);
+    size_t o_cinfo = pl.take<uint16_t>(C);
     size_t o_c64 = pl.take<double>(nchunks), o_cta = pl.take<double>(2 * (size_t)L.cg_blocks);
+    size_t o_plan = pl.take<uint32_t>(nchunks), o_poff = pl.take<uint32_t>(fl::CHUNK + 1);
     size_t o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
     void* pool = nullptr;
     cudaError_t e = cudaMalloc(&pool, pl.off);
@@ -738,10 +744,13 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     b.dB = (float*)(base + o_dB);
     b.q = (float*)(base + o_q);
     b.chunk_flag = (uint8_t*)(base + o_flag);
+    b.cinfo = (uint16_t*)(base + o_cinfo);
     b.part_rr = (float*)(base + o_prr);
     b.part_dq = (float*)(base + o_pdq);
     b.chunk_rr64 = (double*)(base + o_c64);
     b.cta_part64 = (double*)(base + o_cta);
+    b.cg_chunk = (uint32_t*)(base + o_plan);
+    b.cg_off = (uint32_t*)(base + o_poff);
     float* ddiv = (float*)(base + o_div);
     cudaStream_t st = nullptr;
     fl_status rs = FL_OK;

@@ -9,9 +9,9 @@
 // grow the device footprint after start-up.  They pass the inputs and the
 // output as device pointers; this entry point allocates nothing.
 //
-// The scratch (CG vectors r, d (two copies), q, per-chunk partials, the
-// settings block and the device counters) lives in `g_noalloc_scratch`, sized
-// for at most FL_NOALLOC_MAX_CELLS cells (~4.1 MB).  Every GPU that loads this
+// The scratch (CG vectors r, d (two copies), q, the stencil masks, per-chunk
+// partials, the solve plan, the settings block and the device counters) lives in `g_noalloc_scratch`, sized
+// for at most FL_NOALLOC_MAX_CELLS cells (~4.6 MB).  Every GPU that loads this
 // library holds that array until the process exits.  All calls share it: a
 // call keeps the previous call's contents, so the set-up kernel clears what
 // must start at zero (the barrier counter and the status word), and calls that
@@ -50,7 +50,10 @@ constexpr size_t kOffPrr = align256(kOffFlag + kChunks);
 constexpr size_t kOffPdq = align256(kOffPrr + 4 * kChunks);
 constexpr size_t kOffC64 = align256(kOffPdq + 4 * kChunks);
 constexpr size_t kOffCta = align256(kOffC64 + 8 * kChunks);
-constexpr size_t kScratchBytes = align256(kOffCta + 8 * 2 * kMaxCtas);
+constexpr size_t kOffPlan = align256(kOffCta + 8 * 2 * kMaxCtas);
+constexpr size_t kOffPlanOff = align256(kOffPlan + 4 * kChunks);
+constexpr size_t kOffInfo = align256(kOffPlanOff + 4 * (fl::CHUNK + 1));
+constexpr size_t kScratchBytes = align256(kOffInfo + 2 * kCells);
 
 constexpr int kMaxDevices = 64;
 
@@ -165,6 +168,9 @@ extern "C" fl_status fl_solve_pressure_noalloc(uint32_t nx, uint32_t ny, uint32_
     b.part_dq = (float*)(base + kOffPdq);
     b.chunk_rr64 = (double*)(base + kOffC64);
     b.cta_part64 = (double*)(base + kOffCta);
+    b.cg_chunk = (uint32_t*)(base + kOffPlan);
+    b.cg_off = (uint32_t*)(base + kOffPlanOff);
+    b.cinfo = (uint16_t*)(base + kOffInfo);
 
     cudaStream_t st = (cudaStream_t)cuda_stream;
     k_noalloc_setup<<<1, 32, 0, st>>>(d, (fl::DevParams*)(base + kOffParams), b.st);

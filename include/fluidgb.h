@@ -210,7 +210,7 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
  * output are DEVICE pointers: cell types (u8), divergence, and pressure
  * (read as the initial guess when warm_start != 0, overwritten with the
  * result).  The CG scratch is one static device array sized for
- * FL_NOALLOC_MAX_CELLS cells (about 4.1 MB, held by every GPU that loads the
+ * FL_NOALLOC_MAX_CELLS cells (about 4.6 MB, held by every GPU that loads the
  * library until exit); larger grids return FL_INVALID_ARG.  The first call on
  * a device looks up the array's device address (cudaGetSymbolAddress), so make
  * it before any stream capture.  All calls share the array: calls that overlap

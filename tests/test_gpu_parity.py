@@ -198,8 +198,9 @@ def test_fp64_reductions_match_oracle_to_tolerance(lib, oracle):
     assert abs(g.stats()["cg_iterations"] - o.stats()["cg_iterations"]) <= 1
 
 
-def test_gpu_run_is_deterministic(lib):
-    p, parts, _ = scenes.workload("dam32")
+@pytest.mark.parametrize("precision", [0, FL_CG_F64])
+def test_gpu_run_is_deterministic(lib, precision):
+    p, parts, _ = scenes.workload("dam32", precision=precision)
     outs = []
     for _ in range(2):
         g = Fluid(p, parts.shape[0])

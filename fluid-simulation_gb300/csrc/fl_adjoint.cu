@@ -1,0 +1,337 @@
+// fl_adjoint.cu — hand-written adjoint of one substep.
+//
+// The forward substep (fl_bin/fl_grid/fl_cg/fl_g2p) is differentiated with its
+// discrete choices held fixed from the recorded step: the bin permutation, the
+// cell types (and therefore the wet / solid / gradient-face masks), the CFL
+// and wall clamps.  The fixed-point P2G is differentiated as the real-valued
+// weighted mean it approximates (vel_f = sum w v / sum w), linearised at the
+// unquantised sums: where sum w is small (faces at the liquid surface) the
+// 2^-16 quantum of the fixed-point sums is a large fraction of vel_f, and the
+// position derivative dw (v_p - vel_f) / sum w would amplify it.  The pressure
+// solve as the exact linear solve A p = b (A symmetric), so its adjoint is a
+// second CG solve with the same operator.  Stages, in reverse order:
+//
+//   k_adj_g2p       g2p.wgsl:131-198 (forward Euler, friction off): particle
+//                   gradients w.r.t. position and velocity, and face gradients
+//                   of the final and saved velocities (scatter = transpose of
+//                   the trilinear gather; float atomics)
+//   k_adj_prhs      gradient.wgsl transposed: dL/dp per liquid cell, the RHS
+//                   of the adjoint pressure solve A lambda = dL/dp
+//   (k_solve_init + k_cg with the RHS: the adjoint solve)
+//   k_adj_faces     divergence.wgsl and gradient.wgsl transposed, then
+//                   boundaries.wgsl / forces.wgsl / save_vel.wgsl: gradient of
+//                   the normalised P2G face velocity, and dL/dgravity
+//   k_adj_p2g_sums  scatter.wgsl without the fixed-point rounding (float
+//                   atomics): sum w and sum w v per face
+//   k_adj_p2g       scatter.wgsl transposed: a gather from faces to particles
+//                   (velocity and position gradients)
+//   k_adj_unsort    sort_scatter.wgsl transposed: back to the step's input order
+#include "fl_device.cuh"
+
+namespace fl {
+
+__device__ __forceinline__ bool touches_static_a(int axis, int ii, int jj, int kk, int nx, int ny, int nz) {
+    if (axis == 0) return ii <= 1 || ii >= nx - 1 || jj <= 0 || jj >= ny - 1 || kk <= 0 || kk >= nz - 1;
+    if (axis == 1) return ii <= 0 || ii >= nx - 1 || jj <= 1 || jj >= ny - 1 || kk <= 0 || kk >= nz - 1;
+    return ii <= 0 || ii >= nx - 1 || jj <= 0 || jj >= ny - 1 || kk <= 1 || kk >= nz - 1;
+}
+
+// Trilinear stencil of one axis at cell-space point q (forward: scatter.wgsl /
+// g2p.wgsl).  Calls f(face index, w, dw/dq[3]) for each in-range tap.
+template <class Fn>
+__device__ __forceinline__ void stencil(const DevParams& P, int axis, const float q[3], bool wall_aware, Fn f) {
+    const int n3[3] = {(int)P.nx, (int)P.ny, (int)P.nz};
+    int dim[3], base[3];
+    float t[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+        dim[b] = n3[b] + (axis == b ? 1 : 0);
+        const float g = q[b] + (b == axis ? 0.0f : -0.5f);
+        base[b] = __float2int_rz(floorf(g));
+        t[b] = g - (float)base[b];
+    }
+#pragma unroll
+    for (int dk = 0; dk < 2; dk++) {
+        const int kk = base[2] + dk;
+        if (kk < 0 || kk >= dim[2]) continue;
+        const float wz = dk ? t[2] : 1.0f - t[2], sz = dk ? 1.0f : -1.0f;
+#pragma unroll
+        for (int dj = 0; dj < 2; dj++) {
+            const int jj = base[1] + dj;
+            if (jj < 0 || jj >= dim[1]) continue;
+            const float wy = dj ? t[1] : 1.0f - t[1], sy = dj ? 1.0f : -1.0f;
+#pragma unroll
+            for (int di = 0; di < 2; di++) {
+                const int ii = base[0] + di;
+                if (ii < 0 || ii >= dim[0]) continue;
+                if (wall_aware && touches_static_a(axis, ii, jj, kk, n3[0], n3[1], n3[2])) continue;
+                const float wx = di ? t[0] : 1.0f - t[0], sx = di ? 1.0f : -1.0f;
+                const float dw[3] = {sx * wy * wz, wx * sy * wz, wx * wy * sz};
+                const size_t idx = (size_t)ii + (size_t)dim[0] * ((size_t)jj + (size_t)dim[1] * kk);
+                f(idx, wx * wy * wz, dw);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// G2P + advection adjoint (forward Euler, no friction).
+
+__global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
+    const DevParams& P = *a.prm;
+    const uint32_t n = P.n;
+    const float alpha = P.flip, dt = P.dt, maxs = P.maxs, inv_h = P.inv_h;
+    for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
+        const float4 pos = a.part[2 * (size_t)d], pvel = a.part[2 * (size_t)d + 1];
+        const float X[3] = {pos.x, pos.y, pos.z}, pv[3] = {pvel.x, pvel.y, pvel.z};
+        const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
+        // forward recompute: pic, saved, their position derivatives
+        float pic[3], sv[3], dpic[3][3], dsv[3][3];
+        for (int ax = 0; ax < 3; ax++) {
+            float fsum = 0.0f, ssum = 0.0f, wsum = 0.0f, dws[3] = {0, 0, 0}, dfs[3] = {0, 0, 0}, dss[3] = {0, 0, 0};
+            const float* fv = a.fin[ax];
+            const float* svv = a.sav[ax];
+            stencil(P, ax, q, true, [&](size_t idx, float w, const float* dw) {
+                const float f = fv[idx], s = svv[idx];
+                fsum += w * f;
+                ssum += w * s;
+                wsum += w;
+                for (int b = 0; b < 3; b++) {
+                    dws[b] += dw[b];
+                    dfs[b] += dw[b] * f;
+                    dss[b] += dw[b] * s;
+                }
+            });
+            if (wsum > 0.0f) {
+                pic[ax] = fsum / wsum;
+                sv[ax] = ssum / wsum;
+                for (int b = 0; b < 3; b++) {  // d(F/W) = (dF - (F/W) dW)/W, per unit cell coordinate
+                    dpic[ax][b] = (dfs[b] - pic[ax] * dws[b]) / wsum * inv_h;
+                    dsv[ax][b] = (dss[b] - sv[ax] * dws[b]) / wsum * inv_h;
+                }
+            } else {
+                pic[ax] = sv[ax] = 0.0f;
+                for (int b = 0; b < 3; b++) dpic[ax][b] = dsv[ax][b] = 0.0f;
+            }
+        }
+        float mix[3];
+        for (int b = 0; b < 3; b++) mix[b] = pic[b] * (1.0f - alpha) + (pv[b] + (pic[b] - sv[b])) * alpha;
+        const float sp = sqrtf(mix[0] * mix[0] + mix[1] * mix[1] + mix[2] * mix[2]);
+        const bool clamped = sp > maxs && sp > 0.0f;
+        const float sc = clamped ? maxs / sp : 1.0f;
+        float nv[3], np[3];
+        bool wall[3];
+        for (int b = 0; b < 3; b++) {
+            nv[b] = mix[b] * sc;
+            np[b] = X[b] + nv[b] * dt;
+            wall[b] = np[b] < P.lo[b] || np[b] > P.hi[b];
+        }
+        // backward
+        const float4 g0 = a.g_out[2 * (size_t)d], g1 = a.g_out[2 * (size_t)d + 1];
+        const float gnp[3] = {g0.x, g0.y, g0.z}, gnv_out[3] = {g1.x, g1.y, g1.z};
+        float gX[3], gnv[3];
+        for (int b = 0; b < 3; b++) {
+            // clamped component: position pinned to the wall, velocity zeroed
+            gX[b] = wall[b] ? 0.0f : gnp[b];
+            gnv[b] = wall[b] ? 0.0f : gnp[b] * dt + gnv_out[b];
+        }
+        float gmix[3];
+        if (clamped) {  // nv = mix * maxs/|mix|
+            const float inv = 1.0f / sp;
+            const float dotp = (gnv[0] * mix[0] + gnv[1] * mix[1] + gnv[2] * mix[2]) * inv * inv;
+            for (int b = 0; b < 3; b++) gmix[b] = sc * (gnv[b] - mix[b] * dotp);
+        } else {
+            for (int b = 0; b < 3; b++) gmix[b] = gnv[b];
+        }
+        // mix = pic + alpha*(pv - saved)
+        float gpv[3], gpic[3], gsv[3];
+        for (int b = 0; b < 3; b++) {
+            gpic[b] = gmix[b];
+            gpv[b] = alpha * gmix[b];
+            gsv[b] = -alpha * gmix[b];
+        }
+        for (int b = 0; b < 3; b++)
+            for (int ax = 0; ax < 3; ax++) gX[b] += gpic[ax] * dpic[ax][b] + gsv[ax] * dsv[ax][b];
+        // face gradients: pic_ax = sum (w/W) fin_f
+        for (int ax = 0; ax < 3; ax++) {
+            float wsum = 0.0f;
+            stencil(P, ax, q, true, [&](size_t, float w, const float*) { wsum += w; });
+            if (!(wsum > 0.0f)) continue;
+            const float cf = gpic[ax] / wsum, cs = gsv[ax] / wsum;
+            float* gf = a.g_fin[ax];
+            float* gs = a.g_sav[ax];
+            stencil(P, ax, q, true, [&](size_t idx, float w, const float*) {
+                if (cf != 0.0f) atomicAdd(&gf[idx], w * cf);
+                if (cs != 0.0f) atomicAdd(&gs[idx], w * cs);
+            });
+        }
+        a.g_sorted[2 * (size_t)d] = make_float4(gX[0], gX[1], gX[2], 0.0f);
+        a.g_sorted[2 * (size_t)d + 1] = make_float4(gpv[0], gpv[1], gpv[2], 0.0f);
+    }
+}
+
+// Gradient faces: interior, neither side solid, at least one side liquid (gradient.wgsl:45-63).
+__device__ __forceinline__ bool grad_face(uint8_t lt, uint8_t ht) {
+    return lt != CELL_SOLID && ht != CELL_SOLID && (lt == CELL_LIQUID || ht == CELL_LIQUID);
+}
+
+// dL/dp_c = -coeff * (sum over gradient faces whose hi cell is c of g - ... whose lo cell is c).
+__global__ void __launch_bounds__(256) k_adj_prhs(AdjBufs a) {
+    const DevParams& P = *a.prm;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.C) return;
+    float acc = 0.0f;
+    if (a.ct[c] == CELL_LIQUID) {
+        const uint32_t nx = P.nx, ny = P.ny;
+        const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+        const uint32_t ijk[3] = {i, j, k};
+        const size_t step[3] = {1, nx, (size_t)nx * ny};
+        for (int ax = 0; ax < 3; ax++) {
+            const uint32_t dx = face_dim(P, ax, 0), dy = face_dim(P, ax, 1);
+            // face at the low side of c (c is its hi cell) and at the high side (c is its lo cell)
+            for (int side = 0; side < 2; side++) {
+                uint32_t f3[3] = {i, j, k};
+                f3[ax] = ijk[ax] + side;
+                const size_t fidx = (size_t)f3[0] + dx * ((size_t)f3[1] + (size_t)dy * f3[2]);
+                const size_t other = side == 0 ? c - step[ax] : c + step[ax];
+                if (!grad_face(a.ct[side == 0 ? other : c], a.ct[side == 0 ? c : other])) continue;
+                const float g = a.g_fin[ax][fidx];
+                acc += side == 0 ? g : -g;
+            }
+        }
+        acc *= -P.coeff_grad;
+    }
+    a.rhs[c] = acc;
+}
+
+// Face stage: projection (divergence transposed), boundaries, forces, save_vel.
+__global__ void __launch_bounds__(256) k_adj_faces(AdjBufs a, int axis) {
+    __shared__ double s_red[8];
+    const DevParams& P = *a.prm;
+    const uint32_t nf = P.F3[axis];
+    const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+    double gg = 0.0;
+    if (f < nf) {
+        const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
+        const uint32_t i = f % dx, j = (f / dx) % dy, k = f / (dx * dy);
+        const uint32_t comp = axis == 0 ? i : (axis == 1 ? j : k);
+        const uint32_t nax = axis == 0 ? P.nx : (axis == 1 ? P.ny : P.nz);
+        const size_t hi_c = (size_t)i + P.nx * ((size_t)j + (size_t)P.ny * k);
+        const size_t step = axis == 0 ? 1 : (axis == 1 ? P.nx : (size_t)P.nx * P.ny);
+        const uint8_t tl = comp > 0 ? a.ct[hi_c - step] : CELL_SOLID;
+        const uint8_t th = comp < nax ? a.ct[hi_c] : CELL_SOLID;
+        const bool solid = comp == 0 || comp == nax || tl == CELL_SOLID || th == CELL_SOLID;
+        float gpre = 0.0f;
+        if (!solid) {
+            // vel_final = vel_pre - coeff*(p_hi - p_lo) on gradient faces; p = A^-1(-scale*div(vel_pre))
+            float g = a.g_fin[axis][f];
+            float dl = 0.0f;
+            if (tl == CELL_LIQUID) dl += a.lam[hi_c - step];
+            if (th == CELL_LIQUID) dl -= a.lam[hi_c];
+            g += -P.scale_rhs * P.inv_h * dl;
+            gpre = g;
+            const bool wet = tl == CELL_LIQUID || th == CELL_LIQUID;
+            if (wet) gg = (double)gpre * (double)P.dt;
+        }
+        a.g_norm[axis][f] = gpre + a.g_sav[axis][f];
+    }
+    // dL/dg_axis (fixed order within the block, atomics across blocks)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) gg += __shfl_down_sync(0xffffffffu, gg, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = gg;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < 8; w++) s += s_red[w];
+        if (s != 0.0) atomicAdd(&a.g_grav[axis], s);
+    }
+}
+
+// P2G transposed: vel_f = sum_p w v / sum_p w  ->  gather per particle.
+// scatter.wgsl's sums without the fixed-point rounding: the point at which
+// k_adj_p2g linearises the normalisation.  Bin order keeps the atomics of a
+// warp on neighbouring faces.
+__global__ void __launch_bounds__(256) k_adj_p2g_sums(AdjBufs a) {
+    const DevParams& P = *a.prm;
+    const uint32_t n = P.n;
+    const float inv_h = P.inv_h;
+    for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
+        const float4 pos = a.part[2 * (size_t)d], pvel = a.part[2 * (size_t)d + 1];
+        const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
+        const float pv[3] = {pvel.x, pvel.y, pvel.z};
+        for (int ax = 0; ax < 3; ax++) {
+            float* ws = a.w_sum[ax];
+            float* wvs = a.wv_sum[ax];
+            stencil(P, ax, q, false, [&](size_t idx, float w, const float*) {
+                atomicAdd(ws + idx, w);
+                atomicAdd(wvs + idx, w * pv[ax]);
+            });
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_adj_p2g(AdjBufs a) {
+    const DevParams& P = *a.prm;
+    const uint32_t n = P.n;
+    const float inv_h = P.inv_h;
+    for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
+        const float4 pos = a.part[2 * (size_t)d], pvel = a.part[2 * (size_t)d + 1];
+        const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
+        const float pv[3] = {pvel.x, pvel.y, pvel.z};
+        float gX[3] = {0, 0, 0}, gv[3] = {0, 0, 0};
+        for (int ax = 0; ax < 3; ax++) {
+            const float* ws = a.w_sum[ax];
+            const float* wvs = a.wv_sum[ax];
+            const float* gn = a.g_norm[ax];
+            stencil(P, ax, q, false, [&](size_t idx, float w, const float* dw) {
+                const float W = ws[idx];
+                if (!(W > 0.0f)) return;
+                const float g = gn[idx] / W;
+                gv[ax] += w * g;
+                const float diff = (pv[ax] - wvs[idx] / W) * g * inv_h;
+                for (int b = 0; b < 3; b++) gX[b] += dw[b] * diff;
+            });
+        }
+        float4 s0 = a.g_sorted[2 * (size_t)d], s1 = a.g_sorted[2 * (size_t)d + 1];
+        s0.x += gX[0]; s0.y += gX[1]; s0.z += gX[2];
+        s1.x += gv[0]; s1.y += gv[1]; s1.z += gv[2];
+        a.g_sorted[2 * (size_t)d] = s0;
+        a.g_sorted[2 * (size_t)d + 1] = s1;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_adj_unsort(AdjBufs a) {
+    const uint32_t n = a.prm->n;
+    for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
+        const uint32_t src = a.perm[d];
+        a.g_in[2 * (size_t)src] = a.g_sorted[2 * (size_t)d];
+        a.g_in[2 * (size_t)src + 1] = a.g_sorted[2 * (size_t)d + 1];
+    }
+}
+
+cudaError_t launch_adj_g2p(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {
+    k_adj_g2p<<<L.particle_blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s) {
+    k_adj_prhs<<<(C + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_faces(const AdjBufs& a, const uint32_t F3[3], cudaStream_t s) {
+    for (int ax = 0; ax < 3; ax++) k_adj_faces<<<(F3[ax] + 255) / 256, 256, 0, s>>>(a, ax);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_p2g_sums(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {
+    k_adj_p2g_sums<<<L.particle_blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_p2g(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {
+    k_adj_p2g<<<L.particle_blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_unsort(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {
+    k_adj_unsort<<<L.particle_blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace fl

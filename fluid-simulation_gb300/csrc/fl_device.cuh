@@ -90,6 +90,31 @@ struct DevBufs {
     uint32_t* cg_off;      // CG plan: 257 segment offsets into cg_chunk
 };
 
+// Buffers of one adjoint step (fl_adjoint.cu).
+struct AdjBufs {
+    const DevParams* prm;
+    // recorded step
+    const float4* part;      // bin-ordered particles at step start (pos, vel)
+    const uint32_t* perm;    // perm[d] = input slot of sorted particle d
+    const uint8_t* ct;
+    const float* sav[3];     // normalised P2G face velocity (pre-force)
+    const float* fin[3];     // final face velocity (post-projection)
+    // gradients
+    const float4* g_out;     // dL/d(output particle d), bin order, 2 float4 each
+    float4* g_sorted;        // dL/d(input particle in bin order), 2 float4 each
+    float4* g_in;            // dL/d(input particle), input order
+    float* g_fin[3];
+    float* g_sav[3];
+    float* g_norm[3];
+    // Unquantised P2G sums sum w and sum w v of the recorded step (scratch that
+    // aliases g_fin / g_sav once k_adj_faces has consumed those).
+    float* w_sum[3];
+    float* wv_sum[3];
+    float* lam;              // adjoint pressure (the solve's x)
+    float* rhs;              // dL/dp
+    double* g_grav;          // 3 accumulators
+};
+
 // ---------------------------------------------------------------------------
 // helpers (device code only; fl_host.cpp sees the layout above)
 #if defined(__CUDACC__)
@@ -174,6 +199,13 @@ cudaError_t launch_g2p(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_impulse(float4* part, const DevParams* prm, float dx, float dy, float dz,
                            const LaunchCfg& L, cudaStream_t s);
 int cg_max_blocks_per_sm();
+struct AdjBufs;
+cudaError_t launch_adj_g2p(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
+cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s);
+cudaError_t launch_adj_faces(const AdjBufs& a, const uint32_t F3[3], cudaStream_t s);
+cudaError_t launch_adj_p2g_sums(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
+cudaError_t launch_adj_p2g(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
+cudaError_t launch_adj_unsort(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 // Stand-alone CG on prepared cell arrays (used by fl_solve_pressure).
 cudaError_t launch_solve_init(const DevBufs& b, uint32_t C, const float* div, cudaStream_t s);
 }  // namespace fl

@@ -782,6 +782,233 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     return FL_OK;
 }
 
+fl_status fl_get_particles_device(fl_handle* h, void* dst_dev) {
+    if (!h || (!dst_dev && h->n)) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    if (h->n) FL_CUDA(h, cudaMemcpyAsync(dst_dev, h->partA, (size_t)h->n * 32, cudaMemcpyDeviceToDevice, h->stream));
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return read_status(h);
+}
+
+fl_status fl_set_particles_device(fl_handle* h, const void* src_dev, uint32_t n) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (n > h->cap) return set_err(h, FL_INVALID_ARG, "n exceeds the handle capacity");
+    if (n && !src_dev) return set_err(h, FL_INVALID_ARG, "src_dev is NULL");
+    if (n) FL_CUDA(h, cudaMemcpyAsync(h->partA, src_dev, (size_t)n * 32, cudaMemcpyDeviceToDevice, h->stream));
+    if (n != h->n) {
+        h->n = n;
+        fl_status s = upload_params(h);
+        if (s != FL_OK) return s;
+    }
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return FL_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// tapes and the adjoint step
+
+struct fl_tape {
+    fl_handle* h = nullptr;
+    uint32_t max_steps = 0, count = 0;
+    void* pool = nullptr;
+    char* slots = nullptr;
+    size_t slot_bytes = 0, o_part = 0, o_perm = 0, o_ct = 0, o_sav[3] = {}, o_fin[3] = {};
+    float4* g_sorted = nullptr;
+    float* g_fin[3] = {};
+    float* g_sav[3] = {};
+    float* g_norm[3] = {};
+    float* rhs = nullptr;
+    double* g_grav = nullptr;
+    DevBufs cg{};        // buffers of the adjoint pressure solve (cg.p holds lambda)
+    DevParams hp_cg{};
+};
+
+extern "C" {
+
+fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
+    if (!h || !out || max_steps == 0) return set_err(h, FL_INVALID_ARG, "bad argument");
+    *out = nullptr;
+    fl_tape* t = new (std::nothrow) fl_tape();
+    if (!t) return set_err(h, FL_OOM, "host allocation failed");
+    t->h = h;
+    t->max_steps = max_steps;
+    const size_t cap = std::max<uint32_t>(h->cap, 1), C = h->C, nch = h->nchunks;
+    PoolPlan slot;
+    t->o_part = slot.take<float4>(2 * cap);
+    t->o_perm = slot.take<uint32_t>(cap);
+    t->o_ct = slot.take<uint8_t>(C);
+    for (int a = 0; a < 3; a++) {
+        t->o_sav[a] = slot.take<float>(h->F3[a]);
+        t->o_fin[a] = slot.take<float>(h->F3[a]);
+    }
+    t->slot_bytes = (slot.off + 255) & ~size_t(255);
+    PoolPlan pl;
+    pl.off = t->slot_bytes * max_steps;
+    size_t o_gs = pl.take<float4>(2 * cap), o_gf[3], o_gv[3], o_gn[3];
+    for (int a = 0; a < 3; a++) {
+        o_gf[a] = pl.take<float>(h->F3[a]);
+        o_gv[a] = pl.take<float>(h->F3[a]);
+        o_gn[a] = pl.take<float>(h->F3[a]);
+    }
+    size_t o_rhs = pl.take<float>(C), o_lam = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C),
+           o_dB = pl.take<float>(C), o_q = pl.take<float>(C), o_ci = pl.take<uint16_t>(C), o_fl = pl.take<uint8_t>(nch),
+           o_prr = pl.take<float>(nch), o_pdq = pl.take<float>(nch), o_c64 = pl.take<double>(nch),
+           o_cta = pl.take<double>(2 * (size_t)g_num_sms * g_cg_per_sm), o_plan = pl.take<uint32_t>(nch),
+           o_poff = pl.take<uint32_t>(fl::CHUNK + 1), o_gg = pl.take<double>(3), o_prm = pl.take<DevParams>(1),
+           o_st = pl.take<DevStats>(1);
+    cudaError_t e = cudaMalloc(&t->pool, pl.off);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        delete t;
+        return set_err(h, FL_OOM, "tape allocation of " + std::to_string(pl.off) + " bytes failed");
+    }
+    char* base = (char*)t->pool;
+    t->slots = base;
+    t->g_sorted = (float4*)(base + o_gs);
+    for (int a = 0; a < 3; a++) {
+        t->g_fin[a] = (float*)(base + o_gf[a]);
+        t->g_sav[a] = (float*)(base + o_gv[a]);
+        t->g_norm[a] = (float*)(base + o_gn[a]);
+    }
+    t->rhs = (float*)(base + o_rhs);
+    t->g_grav = (double*)(base + o_gg);
+    DevBufs& b = t->cg;
+    b.prm = (DevParams*)(base + o_prm);
+    b.st = (DevStats*)(base + o_st);
+    b.p = (float*)(base + o_lam);
+    b.r = (float*)(base + o_r);
+    b.dA = (float*)(base + o_dA);
+    b.dB = (float*)(base + o_dB);
+    b.q = (float*)(base + o_q);
+    b.cinfo = (uint16_t*)(base + o_ci);
+    b.chunk_flag = (uint8_t*)(base + o_fl);
+    b.part_rr = (float*)(base + o_prr);
+    b.part_dq = (float*)(base + o_pdq);
+    b.chunk_rr64 = (double*)(base + o_c64);
+    b.cta_part64 = (double*)(base + o_cta);
+    b.cg_chunk = (uint32_t*)(base + o_plan);
+    b.cg_off = (uint32_t*)(base + o_poff);
+    *out = t;
+    return FL_OK;
+}
+
+fl_status fl_tape_free(fl_tape* t) {
+    if (!t) return FL_OK;
+    if (t->h && t->h->stream) cudaStreamSynchronize(t->h->stream);
+    if (t->pool) cudaFree(t->pool);
+    delete t;
+    return FL_OK;
+}
+
+fl_status fl_tape_clear(fl_tape* t) {
+    if (!t) return set_err(nullptr, FL_INVALID_ARG, "tape is NULL");
+    t->count = 0;
+    return FL_OK;
+}
+
+fl_status fl_tape_count(const fl_tape* t, uint32_t* n_out) {
+    if (!t || !n_out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    *n_out = t->count;
+    return FL_OK;
+}
+
+fl_status fl_step_record(fl_handle* h, fl_tape* t) {
+    if (!h || !t || t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
+    if (t->count >= t->max_steps) return set_err(h, FL_INVALID_ARG, "tape is full");
+    fl_status s = fl_step(h, 1);
+    if (s != FL_OK) return s;
+    char* slot = t->slots + (size_t)t->count * t->slot_bytes;
+    const size_t n = h->n;
+    cudaStream_t st = h->stream;
+    if (n) {
+        FL_CUDA(h, cudaMemcpyAsync(slot + t->o_part, h->b.part_sorted, 32 * n, cudaMemcpyDeviceToDevice, st));
+        FL_CUDA(h, cudaMemcpyAsync(slot + t->o_perm, h->b.perm, 4 * n, cudaMemcpyDeviceToDevice, st));
+    }
+    FL_CUDA(h, cudaMemcpyAsync(slot + t->o_ct, h->b.ct, h->C, cudaMemcpyDeviceToDevice, st));
+    for (int a = 0; a < 3; a++) {
+        const size_t fb = 4 * (size_t)h->F3[a];
+        FL_CUDA(h, cudaMemcpyAsync(slot + t->o_sav[a], h->b.sav[a], fb, cudaMemcpyDeviceToDevice, st));
+        FL_CUDA(h, cudaMemcpyAsync(slot + t->o_fin[a], h->b.vel[a], fb, cudaMemcpyDeviceToDevice, st));
+    }
+    t->count++;
+    return FL_OK;
+}
+
+fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, void* dL_din_dev, float* dL_dgrav,
+                          uint32_t adj_cg_iters, float adj_cg_tol) {
+    if (!h || !t || t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
+    if (t->count == 0) return set_err(h, FL_INVALID_ARG, "tape is empty");
+    if (h->n && (!dL_dout_dev || !dL_din_dev)) return set_err(h, FL_INVALID_ARG, "gradient buffer is NULL");
+    if (h->prm.advect_order == 2u || h->prm.phys[3] != 0.0f)
+        return set_err(h, FL_INVALID_ARG, "the adjoint supports advect_order 1 and wall_friction 0");
+    const uint32_t k = t->count - 1;
+    char* slot = t->slots + (size_t)k * t->slot_bytes;
+    cudaStream_t st = h->stream;
+    fl::AdjBufs a{};
+    a.prm = h->dprm;
+    a.part = (const float4*)(slot + t->o_part);
+    a.perm = (const uint32_t*)(slot + t->o_perm);
+    a.ct = (const uint8_t*)(slot + t->o_ct);
+    for (int ax = 0; ax < 3; ax++) {
+        a.sav[ax] = (const float*)(slot + t->o_sav[ax]);
+        a.fin[ax] = (const float*)(slot + t->o_fin[ax]);
+        a.g_fin[ax] = t->g_fin[ax];
+        a.g_sav[ax] = t->g_sav[ax];
+        a.g_norm[ax] = t->g_norm[ax];
+        a.w_sum[ax] = t->g_fin[ax];   // free once k_adj_faces has run
+        a.wv_sum[ax] = t->g_sav[ax];
+        FL_CUDA(h, cudaMemsetAsync(t->g_fin[ax], 0, 4 * (size_t)h->F3[ax], st));
+        FL_CUDA(h, cudaMemsetAsync(t->g_sav[ax], 0, 4 * (size_t)h->F3[ax], st));
+    }
+    a.g_out = (const float4*)dL_dout_dev;
+    a.g_sorted = t->g_sorted;
+    a.g_in = (float4*)dL_din_dev;
+    a.lam = t->cg.p;
+    a.rhs = t->rhs;
+    a.g_grav = t->g_grav;
+    FL_CUDA(h, cudaMemsetAsync(t->g_grav, 0, 3 * sizeof(double), st));
+    FL_CUDA(h, fl::launch_adj_g2p(a, h->L, st));
+    FL_CUDA(h, fl::launch_adj_prhs(a, h->C, st));
+    // adjoint pressure solve: A lambda = dL/dp (cold start; k_solve_init's rhs
+    // is -scale*div, so scale = -1 passes dL/dp through unchanged)
+    fl_params q;
+    std::memset(&q, 0, sizeof(q));
+    q.gdim[0] = h->nx; q.gdim[1] = h->ny; q.gdim[2] = h->nz;
+    q.geom[0] = h->prm.geom[0]; q.geom[1] = h->prm.geom[1]; q.geom[2] = h->prm.geom[2]; q.geom[3] = h->prm.geom[3];
+    q.phys[1] = h->prm.phys[1];
+    q.dims[2] = adj_cg_iters ? adj_cg_iters : 1u;
+    q.dims[3] = 0;
+    q.pressure_tolerance = adj_cg_tol;
+    q.cg_precision = FL_CG_F64;
+    derive(q, h->n, t->hp_cg);
+    t->hp_cg.scale_rhs = -1.0f;
+    DevBufs cg = t->cg;
+    cg.ct = const_cast<uint8_t*>(a.ct);
+    FL_CUDA(h, cudaMemcpyAsync((void*)cg.prm, &t->hp_cg, sizeof(DevParams), cudaMemcpyHostToDevice, st));
+    FL_CUDA(h, cudaMemsetAsync(cg.st, 0, sizeof(DevStats), st));
+    FL_CUDA(h, fl::launch_solve_init(cg, h->C, t->rhs, st));
+    FL_CUDA(h, fl::launch_cg(cg, h->L, st));
+    FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));
+    for (int ax = 0; ax < 3; ax++) {
+        FL_CUDA(h, cudaMemsetAsync(a.w_sum[ax], 0, 4 * (size_t)h->F3[ax], st));
+        FL_CUDA(h, cudaMemsetAsync(a.wv_sum[ax], 0, 4 * (size_t)h->F3[ax], st));
+    }
+    FL_CUDA(h, fl::launch_adj_p2g_sums(a, h->L, st));
+    FL_CUDA(h, fl::launch_adj_p2g(a, h->L, st));
+    FL_CUDA(h, fl::launch_adj_unsort(a, h->L, st));
+    double gg[3];
+    DevStats ds;
+    FL_CUDA(h, cudaMemcpyAsync(gg, t->g_grav, sizeof(gg), cudaMemcpyDeviceToHost, st));
+    FL_CUDA(h, cudaMemcpyAsync(&ds, cg.st, sizeof(ds), cudaMemcpyDeviceToHost, st));
+    FL_CUDA(h, cudaStreamSynchronize(st));
+    if (ds.status) return set_err(h, (fl_status)ds.status, "adjoint pressure solve: a device-side wait expired");
+    if (dL_dgrav)
+        for (int i = 0; i < 3; i++) dL_dgrav[i] += (float)gg[i];
+    t->count--;
+    return FL_OK;
+}
+
 const char* fl_last_error(const fl_handle* h) {
     if (h) return h->err.c_str();
     return g_err.c_str();

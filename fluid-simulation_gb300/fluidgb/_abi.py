@@ -100,6 +100,15 @@ SIGNATURES = {
     "fl_solve_pressure_noalloc": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_void_p, c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
                                                  ctypes.c_void_p, ctypes.POINTER(FlStats)]),
+    "fl_get_particles_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_set_particles_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32]),
+    "fl_tape_create": (ctypes.c_int, [ctypes.c_void_p, c_u32, ctypes.POINTER(ctypes.c_void_p)]),
+    "fl_tape_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_tape_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_tape_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32)]),
+    "fl_step_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_step_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _fp, c_u32,
+                                       c_f32]),
     "fl_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
 }
 
@@ -289,6 +298,15 @@ class Fluid:
         self._c(self.lib.fl_get_stats(self.h, ctypes.byref(s)))
         return s.as_dict()
 
+    def get_particles_device(self, ptr):
+        self._c(self.lib.fl_get_particles_device(self.h, ctypes.c_void_p(ptr)))
+
+    def set_particles_device(self, ptr, n):
+        self._c(self.lib.fl_set_particles_device(self.h, ctypes.c_void_p(ptr), n))
+
+    def tape(self, max_steps):
+        return Tape(self, max_steps)
+
     def save_state(self):
         size = ctypes.c_size_t(0)
         self._c(self.lib.fl_save_state(self.h, None, ctypes.byref(size)))
@@ -315,3 +333,42 @@ def solve_pressure(cell_type, div, dims, h, rho, dt, max_iters, warm_start=False
                                       _f32p(pin), _f32p(pout), h, rho, dt, max_iters, 1 if warm_start else 0,
                                       tolerance, precision, ctypes.byref(st)))
     return pout, st.as_dict()
+
+
+class Tape:
+    """Recorded substeps of a handle, for the adjoint (fl_tape_*)."""
+
+    def __init__(self, fluid, max_steps):
+        self.fluid = fluid
+        t = ctypes.c_void_p()
+        fluid._c(fluid.lib.fl_tape_create(fluid.h, max_steps, ctypes.byref(t)))
+        self.t = t
+
+    def close(self):
+        if self.t:
+            self.fluid.lib.fl_tape_free(self.t)
+            self.t = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def clear(self):
+        self.fluid._c(self.fluid.lib.fl_tape_clear(self.t))
+
+    def __len__(self):
+        n = c_u32()
+        self.fluid._c(self.fluid.lib.fl_tape_count(self.t, ctypes.byref(n)))
+        return n.value
+
+    def record(self):
+        self.fluid._c(self.fluid.lib.fl_step_record(self.fluid.h, self.t))
+
+    def adjoint(self, g_out_ptr, g_in_ptr, cg_iters=1000, cg_tol=1e-6):
+        """Pop one step: dL/dout (device ptr) -> dL/din (device ptr); returns dL/dgravity."""
+        gg = (ctypes.c_float * 3)(0.0, 0.0, 0.0)
+        self.fluid._c(self.fluid.lib.fl_step_adjoint(self.fluid.h, self.t, ctypes.c_void_p(g_out_ptr),
+                                                     ctypes.c_void_p(g_in_ptr), gg, cg_iters, cg_tol))
+        return [gg[0], gg[1], gg[2]]

@@ -103,13 +103,27 @@ int orc_get_threads(void) {
 #undef r2i_floor
 
 /* ---------------- f64 instantiation: the same step in double ---------------- */
+/* P2G accumulates in double: integral values (the fixed-point rounding of
+ * scatter.wgsl, exact sums below 2^53) by default, or the unrounded terms when
+ * exact P2G is on — the smooth forward used for finite differences. */
+static int g_exact_p2g = 0;
+void orc_set_exact_p2g(int on) { g_exact_p2g = on != 0; }
+static inline double f64_acc_term(double x) { return g_exact_p2g ? x : (double)d2l_rn_sat(x); }
+static inline void atomic_add_f64(double* p, double v) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+    *p += v;
+}
+#undef ATOMIC_ADD_ACC
+#define ATOMIC_ADD_ACC(ptr, v) atomic_add_f64((ptr), (v))
 #define R double
 #define SFX _f64
 #define IS_F32 0
-#define ACC int64_t
-#define TO_ACC(x) d2l_rn_sat(x)
-#define ACC_TO_R(a) ((double)(a))
-#define ACC_POSITIVE(a) ((a) > 0)
+#define ACC double
+#define TO_ACC(x) f64_acc_term(x)
+#define ACC_TO_R(a) (a)
+#define ACC_POSITIVE(a) ((a) > 0.0)
 #define FLOOR floor
 #define FMIN fmin
 #define FMAX fmax

@@ -43,6 +43,10 @@ typedef struct orc_handle_f64 orc_handle_f64;
                           uint32_t* perm);                                                       \
     int orc_get_stats##SFX(orc_handle##SFX* h, fl_stats* s);                                     \
     int orc_get_divergence##SFX(orc_handle##SFX* h, float* out);                                 \
+    int orc_set_gravity_d##SFX(orc_handle##SFX* h, const double g[3]);                           \
+    int orc_add_velocity_d##SFX(orc_handle##SFX* h, const double* dv, double eps);               \
+    int orc_mean_position_d##SFX(orc_handle##SFX* h, double out[3]);                             \
+    int orc_add_position_d##SFX(orc_handle##SFX* h, const double* dx, double eps);               \
     int orc_solve_pressure##SFX(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* ct,        \
                                 const float* div, const float* p_in, float* p_out, float h,      \
                                 float rho, float dt, uint32_t max_iters, uint32_t warm,          \
@@ -50,6 +54,10 @@ typedef struct orc_handle_f64 orc_handle_f64;
 
 ORC_DECL(_f32)
 ORC_DECL(_f64)
+
+/* _f64 only: 1 = accumulate P2G terms unrounded (a smooth forward for finite
+ * differences), 0 = the reference's 2^16 fixed-point rounding (default). */
+void orc_set_exact_p2g(int on);
 
 /* Number of OpenMP threads the oracle uses (0 = library default). */
 void orc_set_threads(int n);

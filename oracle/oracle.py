@@ -57,6 +57,10 @@ def load(build=True):
             "orc_get_bins": [ctypes.c_void_p, _u32p_t, _u32p_t, _u32p_t],
             "orc_get_stats": [ctypes.c_void_p, ctypes.POINTER(FlStats)],
             "orc_get_divergence": [ctypes.c_void_p, _fp],
+            "orc_set_gravity_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)],
+            "orc_add_velocity_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_double],
+            "orc_mean_position_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)],
+            "orc_add_position_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_double],
             "orc_solve_pressure": [_u32, _u32, _u32, _u8p_t, _fp, _fp, _fp, ctypes.c_float, ctypes.c_float,
                                    ctypes.c_float, _u32, _u32, ctypes.c_float, _u32, ctypes.POINTER(FlStats)],
         }
@@ -64,6 +68,7 @@ def load(build=True):
             fn = getattr(lib, name + sfx)
             fn.argtypes = args
             fn.restype = ctypes.c_int
+    lib.orc_set_exact_p2g.argtypes = [ctypes.c_int]
     lib.orc_set_threads.argtypes = [ctypes.c_int]
     lib.orc_get_threads.restype = ctypes.c_int
     lib.orc_ref_cell_key.restype = _u32
@@ -108,6 +113,11 @@ def u8p(a):
 
 def set_threads(n):
     load().orc_set_threads(int(n))
+
+
+def set_exact_p2g(on):
+    """_f64 oracle: unrounded P2G accumulation (smooth forward for finite differences)."""
+    load().orc_set_exact_p2g(1 if on else 0)
 
 
 class OracleFluid:
@@ -189,6 +199,23 @@ class OracleFluid:
         v.offsets = u32p(g["offsets"])
         self._c(self._f("orc_get_grid")(self.h, ctypes.byref(v)))
         return g
+
+    def set_gravity_d(self, g):
+        a = np.ascontiguousarray(g, np.float64)
+        self._c(self._f("orc_set_gravity_d")(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+
+    def add_velocity_d(self, dv, eps):
+        a = np.ascontiguousarray(dv, np.float64).reshape(-1, 3)
+        self._c(self._f("orc_add_velocity_d")(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), eps))
+
+    def add_position_d(self, dx, eps):
+        a = np.ascontiguousarray(dx, np.float64).reshape(-1, 3)
+        self._c(self._f("orc_add_position_d")(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), eps))
+
+    def mean_position_d(self):
+        out = np.zeros(3, np.float64)
+        self._c(self._f("orc_mean_position_d")(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return out
 
     def get_divergence(self):
         out = np.empty(self.C, np.float32)

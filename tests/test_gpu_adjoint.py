@@ -1,0 +1,164 @@
+"""Adjoint of the substep (fl_step_record / fl_step_adjoint) against central
+finite differences of the FP64 oracle forward.
+
+Loss: squared distance of the particle centre of mass to a target after a
+short rollout; gradients w.r.t. the initial per-particle velocity and the
+gravity vector, through the checkpointed rollout and torch.autograd.Function.
+The finite-difference forward is the oracle's double-precision step with
+unrounded P2G accumulation and a tight CG (a smooth function of its inputs);
+the adjoint linearises the GPU forward (f32 state, FP64 CG reductions), with
+the P2G normalisation taken at its unquantised sums.  Without that, the 2^16
+fixed-point quantum at low-weight surface faces, amplified by 1/sum(w) in the
+position derivative, put the 4-step gradient off by 66%.
+"""
+import numpy as np
+import pytest
+
+from fluidgb import FL_CG_F64, scenes
+
+pytestmark = pytest.mark.gpu
+
+TARGET = np.array([0.7, 0.2, 0.5])
+
+
+def blob(x, y, z):
+    return (x > 0.3) & (x < 0.7) & (y > 0.35) & (y < 0.65) & (z > 0.3) & (z < 0.7)
+
+
+def setup_case(n=20, steps=4, seed=11):
+    """A blob falling freely, away from the walls (no wall clamps in the run)."""
+    p = scenes.params_for(n, iters=500, tol=1e-6, precision=FL_CG_F64, stiffness=0.0)
+    parts = scenes.seed_particles(n, blob, seed=seed, vel_sigma=0.1)
+    return p, parts, steps
+
+
+def oracle_run(oracle, p, parts, steps, dv, eps, grav, dx=None):
+    """FP64 oracle rollout from `parts` with velocity + eps*dv (and position
+    + eps*dx) and gravity `grav` applied in double: (loss, cell types of every step)."""
+    q = p.copy()
+    q.dims[2] = 3000
+    q.pressure_tolerance = 1e-9
+    o = oracle.OracleFluid(q, parts.shape[0], "f64")
+    o.set_particles(parts)
+    o.set_gravity_d(grav)
+    if dv is not None:
+        o.add_velocity_d(dv, eps)
+    if dx is not None:
+        o.add_position_d(dx, eps)
+    cts = []
+    for _ in range(steps):
+        o.step(1)
+        cts.append(o.get_grid()["cell_type"].copy())
+    c = o.mean_position_d()
+    o.close()
+    return float(((c - TARGET) ** 2).sum()), np.concatenate(cts)
+
+
+def adjoint_grads(p, parts, steps, k):
+    import torch
+    from fluidgb.autograd import Rollout, RolloutFunction, com_loss
+    roll = Rollout(p, parts.shape[0], steps, checkpoint_every=k, adj_cg_iters=3000, adj_cg_tol=1e-7)
+    vel0 = torch.tensor(parts[:, 4:7], device="cuda", requires_grad=True)
+    grav = torch.tensor([0.0, -9.81, 0.0], device="cuda", dtype=torch.float32, requires_grad=True)
+    pos0 = torch.tensor(parts[:, 0:3], device="cuda")
+    final = RolloutFunction.apply(vel0, grav, pos0, roll)
+    loss = com_loss(final, torch.tensor(TARGET, dtype=torch.float32, device="cuda"))
+    loss.backward()
+    roll.close()
+    return vel0.grad.detach().cpu().numpy().astype(np.float64), grav.grad.detach().cpu().numpy().astype(np.float64)
+
+
+@pytest.mark.parametrize("steps,k", [(1, 1), (4, 2), (12, 4)])
+def test_adjoint_matches_finite_differences(oracle, steps, k):
+    pytest.importorskip("torch")
+    from fluidgb import build
+    build.build()
+    p, parts, _ = setup_case(steps=steps)
+    n = parts.shape[0]
+    gv, gg = adjoint_grads(p, parts, steps, k)
+    assert np.all(np.isfinite(gv)) and np.all(np.isfinite(gg))
+    oracle.set_exact_p2g(True)
+    try:
+        base_g = np.array([0.0, np.float32(-9.81), 0.0], np.float64)
+        _, ct0 = oracle_run(oracle, p, parts, steps, None, 0.0, base_g)
+        rng = np.random.default_rng(3)
+        eps = 1e-6  # converged: 1e-5 .. 1e-7 agree to ~1e-5 relative on this scene
+        errs = []
+        tries = 0
+        while len(errs) < 3 and tries < 12:
+            tries += 1
+            dv = rng.standard_normal((n, 3))
+            dg = rng.standard_normal(3)
+            lp, ctp = oracle_run(oracle, p, parts, steps, dv, eps, base_g + eps * dg)
+            lm, ctm = oracle_run(oracle, p, parts, steps, dv, -eps, base_g - eps * dg)
+            if not (np.array_equal(ctp, ct0) and np.array_equal(ctm, ct0)):
+                continue  # a cell changed type between the runs: redraw the direction
+            fd = (lp - lm) / (2 * eps)
+            ad = float((gv * dv).sum() + (gg * dg).sum())
+            errs.append(abs(ad - fd) / max(abs(fd), 1e-12))
+            print("steps %d: adjoint %.6e  fd %.6e  rel err %.2e" % (steps, ad, fd, errs[-1]))
+    finally:
+        oracle.set_exact_p2g(False)
+    assert len(errs) >= 2
+    assert max(errs) < 1e-2, errs
+
+
+def test_checkpointed_recompute_matches_forward():
+    """The backward pass recomputes segments from checkpoints; the recomputed
+    final state must equal the forward's bit for bit."""
+    torch = pytest.importorskip("torch")
+    from fluidgb.autograd import Rollout
+    p, parts, steps = setup_case(steps=5)
+    roll = Rollout(p, parts.shape[0], steps, checkpoint_every=2)
+    final, ids = roll.forward(parts, (0.0, -9.81, 0.0))
+    roll.fluid.load_state(roll.checkpoints[4])
+    roll.fluid.step(1)
+    again, ids2 = roll.fluid.get_particles()
+    assert np.array_equal(final, again) and np.array_equal(ids, ids2)
+    roll.close()
+
+
+@pytest.mark.parametrize("steps,k,what", [(1, 1, "pos"), (2, 1, "vel"), (4, 4, "vel"), (4, 2, "grav")])
+def test_adjoint_position_and_chain_diagnostics(oracle, steps, k, what):
+    """Directional derivatives w.r.t. initial positions (one step), initial
+    velocities (2 and 4 steps, with and without checkpoints) and gravity, each
+    alone: a failure here names the part of the chain that is off."""
+    pytest.importorskip("torch")
+    import torch
+    from fluidgb.autograd import Rollout
+    p, parts, _ = setup_case(steps=steps)
+    n = parts.shape[0]
+    roll = Rollout(p, n, steps, checkpoint_every=k, adj_cg_iters=3000, adj_cg_tol=1e-7)
+    final, ids = roll.forward(parts, (0.0, np.float32(-9.81), 0.0))
+    c = final[:, 0:3].astype(np.float64).mean(axis=0)
+    g = np.zeros((n, 8), np.float32)
+    g[:, 0:3] = (2.0 * (c - TARGET) / n).astype(np.float32)
+    g0, g_grav = roll.backward(g, ids)
+    roll.close()
+    oracle.set_exact_p2g(True)
+    try:
+        base_g = np.array([0.0, np.float32(-9.81), 0.0], np.float64)
+        rng = np.random.default_rng(5)
+        d = rng.standard_normal((n, 3))
+        eps = 1e-6
+        if what == "pos":
+            eps = 1e-7  # tent weights are piecewise linear: keep clear of the kinks
+            lp, _ = oracle_run(oracle, p, parts, steps, None, eps, base_g, dx=d)
+            lm, _ = oracle_run(oracle, p, parts, steps, None, -eps, base_g, dx=d)
+            fd = (lp - lm) / (2 * eps)
+            ad = float((g0[:, 0:3].astype(np.float64) * d).sum())
+        elif what == "grav":
+            dg = np.array([0.3, -1.0, 0.2])
+            lp, _ = oracle_run(oracle, p, parts, steps, None, 0.0, base_g + eps * dg)
+            lm, _ = oracle_run(oracle, p, parts, steps, None, 0.0, base_g - eps * dg)
+            fd = (lp - lm) / (2 * eps)
+            ad = float((np.asarray(g_grav) * dg).sum())
+        else:
+            lp, _ = oracle_run(oracle, p, parts, steps, d, eps, base_g)
+            lm, _ = oracle_run(oracle, p, parts, steps, d, -eps, base_g)
+            fd = (lp - lm) / (2 * eps)
+            ad = float((g0[:, 4:7].astype(np.float64) * d).sum())
+    finally:
+        oracle.set_exact_p2g(False)
+    print("%s steps %d k %d: adjoint %.6e fd %.6e rel %.2e" % (what, steps, k, ad, fd, abs(ad - fd) / abs(fd)))
+    assert abs(ad - fd) <= 1e-2 * abs(fd)

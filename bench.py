@@ -32,7 +32,8 @@ import time
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path[:0] = [os.path.join(REPO, "fluid-simulation_gb300")]
 
-KERNELS_PER_STEP = 15  # bin 8 (count, scan x3, scatter, fix, fix_big, gather), classify, p2g 2, prep, cg, project, g2p
+# bin 8 (count, scan x3, scatter, fix, fix_big, gather), classify, p2g 2, prep, cg plan, cg, project, g2p
+KERNELS_PER_STEP = 16
 
 
 def parse():
@@ -48,6 +49,8 @@ def parse():
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--adj-steps", type=int, default=20, help="rollout length of the forward+adjoint leg (0 = off)")
+    ap.add_argument("--adj-every", type=int, default=10, help="checkpoint interval of that rollout")
     return ap.parse_args()
 
 
@@ -199,6 +202,56 @@ def timed_steps(torch, g, k):
     return e0.elapsed_time(e1)
 
 
+def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol):
+    """Forward+adjoint of a checkpointed rollout against its forward alone.
+
+    forward: `steps` substeps from `parts` with a device checkpoint every
+    `every`, the last segment recorded on the tape; backward: per earlier
+    segment, restore + recompute while recording; every step popped through
+    the adjoint (second CG with the forward's iteration cap, tolerance and
+    precision).  Loss: |centre of mass - (0.7, 0.2, 0.5)|^2.  Timed with CUDA
+    events on the rollout's stream."""
+    from fluidgb.autograd import Rollout
+    n = parts.shape[0]
+    free0 = torch.cuda.mem_get_info()[0]
+    roll = Rollout(p, n, steps, checkpoint_every=every, adj_cg_iters=cg_iters, adj_cg_tol=cg_tol)
+    parts_d = torch.from_numpy(parts).cuda()
+    target = torch.tensor([0.7, 0.2, 0.5], dtype=torch.float64, device="cuda")
+    grav = (p.grav[0], p.grav[1], p.grav[2])
+
+    def loss_grad(final):
+        c = final[:, 0:3].double().mean(dim=0)
+        g = torch.zeros((n, 8), dtype=torch.float32, device="cuda")
+        g[:, 0:3] = (2.0 * (c - target) / n).float()
+        return g
+
+    def once():
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record(roll.stream)
+        final, _ = roll.forward(parts_d, grav)
+        e[1].record(roll.stream)
+        g = loss_grad(final)
+        roll.stream.wait_stream(torch.cuda.current_stream())
+        roll.backward(g)
+        e[2].record(roll.stream)
+        torch.cuda.synchronize()
+        return e[0].elapsed_time(e[1]), e[1].elapsed_time(e[2])
+
+    once()  # warm: graph capture, tape pool
+    fwd_ms, bwd_ms = once()
+    iters = roll.adj_cg_iterations
+    used = free0 - torch.cuda.mem_get_info()[0]
+    roll.close()
+    return {"workload_steps": steps, "checkpoint_every": every,
+            "fwd_ms_per_step": fwd_ms / steps, "fwd_adj_ms_per_step": (fwd_ms + bwd_ms) / steps,
+            "ratio": (fwd_ms + bwd_ms) / fwd_ms,
+            "backward": "last segment taped during the forward; earlier segments restore + recompute-with-tape; adjoint per step",
+            "adj_cg_iters_mean": float(sum(iters)) / max(len(iters), 1), "adj_cg_iters_max": max(iters or [0]),
+            "adj_cg_max_iters": cg_iters, "adj_cg_tol": cg_tol,
+            "device_bytes": used, "device_bytes_note": "handle + tape + checkpoints + torch buffers of the rollout"}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -265,6 +318,11 @@ def run_ours(args):
                 "overhead_pct": 100.0 * (ms64 - ms) / ms, "last_cg_iterations": s64["cg_iterations"]}
         g64.close()
 
+    adj = None
+    if args.adj_steps > 0:
+        adj = adjoint_leg(torch, p, parts, args.adj_steps, args.adj_every, spec["iters"], spec["tol"])
+        torch.cuda.set_stream(stream)
+
     # Per-stage device times (CUDA events between stages on the same stream).
     g.set_profiling(True)
     g.reset_stage_times()
@@ -318,7 +376,7 @@ def run_ours(args):
 
     if rank == 0:
         line = {
-            "metric": "FLIP steps/s @128^3 ~2M particles",
+            "metric": "FLIP steps/s @128^3 ~2M particles; fwd+adjoint/fwd ratio; CG HBM GB/s",
             "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if prec == fluidgb.FL_CG_F32 else "f32+f64-reductions",
@@ -338,6 +396,7 @@ def run_ours(args):
                          "avg_liquid_cells": liquid_avg, "avg_cg_iterations": iters_avg},
             "stage_ms_per_step": {k: v / max(nprof, 1) for k, v in stage_ms.items()},
             "fp64_reductions": fp64,
+            "fwd_adjoint": adj,
             "cpu_baseline": cb,
             "clocks": clock_rec,
             "gpu_launches": KERNELS_PER_STEP * args.steps,

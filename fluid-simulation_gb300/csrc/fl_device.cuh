@@ -196,6 +196,7 @@ cudaError_t launch_grid_prep(const DevBufs& b, uint32_t C, cudaStream_t s);
 cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_project(const DevBufs& b, uint32_t C, cudaStream_t s);
 cudaError_t launch_g2p(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
+cudaError_t launch_iota(uint32_t* ids, uint32_t n, cudaStream_t s);
 cudaError_t launch_impulse(float4* part, const DevParams* prm, float dx, float dy, float dz,
                            const LaunchCfg& L, cudaStream_t s);
 int cg_max_blocks_per_sm();

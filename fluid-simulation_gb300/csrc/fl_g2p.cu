@@ -4,6 +4,8 @@
 // neighbouring threads gather neighbouring faces).  advect_order == 2 adds a
 // midpoint step through the final grid velocity (an extension; the reference
 // advects with forward Euler, g2p.wgsl:186).
+#include <algorithm>
+
 #include "fl_device.cuh"
 
 namespace fl {
@@ -149,6 +151,17 @@ __global__ void __launch_bounds__(256) k_impulse(float4* part, const DevParams* 
         v.w = __fadd_rn(v.w, 0.0f);
         part[2 * (size_t)p + 1] = v;
     }
+}
+
+__global__ void __launch_bounds__(256) k_iota(uint32_t* ids, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) ids[i] = i;
+}
+
+cudaError_t launch_iota(uint32_t* ids, uint32_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t blocks = std::min<uint32_t>((n + 255) / 256, 4096u);
+    k_iota<<<blocks, 256, 0, s>>>(ids, n);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_g2p(const DevBufs& b, const LaunchCfg& L, cudaStream_t s) {

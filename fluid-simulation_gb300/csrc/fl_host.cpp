@@ -693,6 +693,58 @@ fl_status fl_load_state(fl_handle* h, const void* buf, size_t size) {
     return FL_OK;
 }
 
+fl_status fl_save_state_device(fl_handle* h, void* dst_dev, size_t* size_inout) {
+    if (!h || !size_inout) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    const size_t need = sizeof(StateHeader) + (size_t)h->n * 36 + 4 * (size_t)h->C;
+    if (!dst_dev) {
+        *size_inout = need;
+        return FL_OK;
+    }
+    if (*size_inout < need) return set_err(h, FL_INVALID_ARG, "buffer too small");
+    if ((uintptr_t)dst_dev & 15u) return set_err(h, FL_INVALID_ARG, "device state buffer must be 16-byte aligned");
+    StateHeader hd{};
+    std::memcpy(hd.magic, "FLGBSTAT", 8);
+    hd.version = 1; hd.nx = h->nx; hd.ny = h->ny; hd.nz = h->nz; hd.n = h->n; hd.substeps = h->substeps;
+    char* p = (char*)dst_dev;
+    // pageable source: the call returns once `hd` has been staged
+    FL_CUDA(h, cudaMemcpyAsync(p, &hd, sizeof(hd), cudaMemcpyHostToDevice, h->stream));
+    p += sizeof(hd);
+    if (h->n) {
+        FL_CUDA(h, cudaMemcpyAsync(p, h->partA, (size_t)h->n * 32, cudaMemcpyDeviceToDevice, h->stream));
+        p += (size_t)h->n * 32;
+        FL_CUDA(h, cudaMemcpyAsync(p, h->idsA, (size_t)h->n * 4, cudaMemcpyDeviceToDevice, h->stream));
+        p += (size_t)h->n * 4;
+    }
+    FL_CUDA(h, cudaMemcpyAsync(p, h->b.p, 4 * (size_t)h->C, cudaMemcpyDeviceToDevice, h->stream));
+    *size_inout = need;
+    return FL_OK;
+}
+
+fl_status fl_load_state_device(fl_handle* h, const void* src_dev, size_t size) {
+    if (!h || !src_dev) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    if (size < sizeof(StateHeader)) return set_err(h, FL_INVALID_ARG, "state blob too small");
+    StateHeader hd;
+    FL_CUDA(h, cudaMemcpyAsync(&hd, src_dev, sizeof(hd), cudaMemcpyDeviceToHost, h->stream));
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    if (std::memcmp(hd.magic, "FLGBSTAT", 8) != 0 || hd.version != 1)
+        return set_err(h, FL_INVALID_ARG, "not a state blob of this library");
+    if (hd.nx != h->nx || hd.ny != h->ny || hd.nz != h->nz) return set_err(h, FL_INVALID_ARG, "grid mismatch");
+    if (hd.n > h->cap) return set_err(h, FL_INVALID_ARG, "particle count exceeds capacity");
+    const size_t need = sizeof(StateHeader) + (size_t)hd.n * 36 + 4 * (size_t)h->C;
+    if (size < need) return set_err(h, FL_INVALID_ARG, "state blob truncated");
+    const char* p = (const char*)src_dev + sizeof(hd);
+    h->n = hd.n;
+    if (h->n) {
+        FL_CUDA(h, cudaMemcpyAsync(h->partA, p, (size_t)h->n * 32, cudaMemcpyDeviceToDevice, h->stream));
+        p += (size_t)h->n * 32;
+        FL_CUDA(h, cudaMemcpyAsync(h->idsA, p, (size_t)h->n * 4, cudaMemcpyDeviceToDevice, h->stream));
+        p += (size_t)h->n * 4;
+    }
+    FL_CUDA(h, cudaMemcpyAsync(h->b.p, p, 4 * (size_t)h->C, cudaMemcpyDeviceToDevice, h->stream));
+    h->substeps = hd.substeps;
+    return upload_params(h);
+}
+
 fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type, const float* divergence,
                             const float* pressure_in, float* pressure_out, float h, float rho, float dt,
                             uint32_t max_iters, uint32_t warm_start, float tolerance, uint32_t cg_precision,
@@ -782,9 +834,11 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     return FL_OK;
 }
 
-fl_status fl_get_particles_device(fl_handle* h, void* dst_dev) {
+fl_status fl_get_particles_device(fl_handle* h, void* dst_dev, uint32_t* ids_dev) {
     if (!h || (!dst_dev && h->n)) return set_err(h, FL_INVALID_ARG, "NULL argument");
     if (h->n) FL_CUDA(h, cudaMemcpyAsync(dst_dev, h->partA, (size_t)h->n * 32, cudaMemcpyDeviceToDevice, h->stream));
+    if (h->n && ids_dev)
+        FL_CUDA(h, cudaMemcpyAsync(ids_dev, h->idsA, (size_t)h->n * 4, cudaMemcpyDeviceToDevice, h->stream));
     FL_CUDA(h, cudaStreamSynchronize(h->stream));
     return read_status(h);
 }
@@ -794,6 +848,7 @@ fl_status fl_set_particles_device(fl_handle* h, const void* src_dev, uint32_t n)
     if (n > h->cap) return set_err(h, FL_INVALID_ARG, "n exceeds the handle capacity");
     if (n && !src_dev) return set_err(h, FL_INVALID_ARG, "src_dev is NULL");
     if (n) FL_CUDA(h, cudaMemcpyAsync(h->partA, src_dev, (size_t)n * 32, cudaMemcpyDeviceToDevice, h->stream));
+    FL_CUDA(h, fl::launch_iota(h->idsA, n, h->stream));
     if (n != h->n) {
         h->n = n;
         fl_status s = upload_params(h);
@@ -822,6 +877,7 @@ struct fl_tape {
     double* g_grav = nullptr;
     DevBufs cg{};        // buffers of the adjoint pressure solve (cg.p holds lambda)
     DevParams hp_cg{};
+    fl_stats last{};     // of the last adjoint pressure solve
 };
 
 extern "C" {
@@ -913,6 +969,12 @@ fl_status fl_tape_count(const fl_tape* t, uint32_t* n_out) {
     return FL_OK;
 }
 
+fl_status fl_tape_last_stats(const fl_tape* t, fl_stats* out) {
+    if (!t || !out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    *out = t->last;
+    return FL_OK;
+}
+
 fl_status fl_step_record(fl_handle* h, fl_tape* t) {
     if (!h || !t || t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
     if (t->count >= t->max_steps) return set_err(h, FL_INVALID_ARG, "tape is full");
@@ -980,7 +1042,7 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     q.dims[2] = adj_cg_iters ? adj_cg_iters : 1u;
     q.dims[3] = 0;
     q.pressure_tolerance = adj_cg_tol;
-    q.cg_precision = FL_CG_F64;
+    q.cg_precision = h->prm.cg_precision;
     derive(q, h->n, t->hp_cg);
     t->hp_cg.scale_rhs = -1.0f;
     DevBufs cg = t->cg;
@@ -1002,6 +1064,12 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     FL_CUDA(h, cudaMemcpyAsync(gg, t->g_grav, sizeof(gg), cudaMemcpyDeviceToHost, st));
     FL_CUDA(h, cudaMemcpyAsync(&ds, cg.st, sizeof(ds), cudaMemcpyDeviceToHost, st));
     FL_CUDA(h, cudaStreamSynchronize(st));
+    t->last = fl_stats{};
+    t->last.liquid_cells = ds.liquid;
+    t->last.cg_iterations = ds.cg_iters;
+    t->last.device_status = ds.status;
+    t->last.rs_initial = ds.rs_init;
+    t->last.rs_final = ds.rs_final;
     if (ds.status) return set_err(h, (fl_status)ds.status, "adjoint pressure solve: a device-side wait expired");
     if (dL_dgrav)
         for (int i = 0; i < 3; i++) dL_dgrav[i] += (float)gg[i];

@@ -100,12 +100,15 @@ SIGNATURES = {
     "fl_solve_pressure_noalloc": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_void_p, c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
                                                  ctypes.c_void_p, ctypes.POINTER(FlStats)]),
-    "fl_get_particles_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_get_particles_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_save_state_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_size_t)]),
+    "fl_load_state_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
     "fl_set_particles_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32]),
     "fl_tape_create": (ctypes.c_int, [ctypes.c_void_p, c_u32, ctypes.POINTER(ctypes.c_void_p)]),
     "fl_tape_free": (ctypes.c_int, [ctypes.c_void_p]),
     "fl_tape_clear": (ctypes.c_int, [ctypes.c_void_p]),
     "fl_tape_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32)]),
+    "fl_tape_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fl_step_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fl_step_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _fp, c_u32,
                                        c_f32]),
@@ -298,8 +301,8 @@ class Fluid:
         self._c(self.lib.fl_get_stats(self.h, ctypes.byref(s)))
         return s.as_dict()
 
-    def get_particles_device(self, ptr):
-        self._c(self.lib.fl_get_particles_device(self.h, ctypes.c_void_p(ptr)))
+    def get_particles_device(self, ptr, ids_ptr=None):
+        self._c(self.lib.fl_get_particles_device(self.h, ctypes.c_void_p(ptr), ctypes.c_void_p(ids_ptr)))
 
     def set_particles_device(self, ptr, n):
         self._c(self.lib.fl_set_particles_device(self.h, ctypes.c_void_p(ptr), n))
@@ -317,6 +320,19 @@ class Fluid:
     def load_state(self, blob):
         buf = ctypes.create_string_buffer(blob, len(blob))
         self._c(self.lib.fl_load_state(self.h, buf, len(blob)))
+
+    def state_size(self):
+        size = ctypes.c_size_t(0)
+        self._c(self.lib.fl_save_state(self.h, None, ctypes.byref(size)))
+        return size.value
+
+    def save_state_device(self, ptr, size):
+        sz = ctypes.c_size_t(size)
+        self._c(self.lib.fl_save_state_device(self.h, ctypes.c_void_p(ptr), ctypes.byref(sz)))
+        return sz.value
+
+    def load_state_device(self, ptr, size):
+        self._c(self.lib.fl_load_state_device(self.h, ctypes.c_void_p(ptr), size))
 
 
 def solve_pressure(cell_type, div, dims, h, rho, dt, max_iters, warm_start=False, pressure_in=None,
@@ -365,6 +381,11 @@ class Tape:
 
     def record(self):
         self.fluid._c(self.fluid.lib.fl_step_record(self.fluid.h, self.t))
+
+    def last_stats(self):
+        st = FlStats()
+        self.fluid._c(self.fluid.lib.fl_tape_last_stats(self.t, ctypes.byref(st)))
+        return st.as_dict()
 
     def adjoint(self, g_out_ptr, g_in_ptr, cg_iters=1000, cg_tol=1e-6):
         """Pop one step: dL/dout (device ptr) -> dL/din (device ptr); returns dL/dgravity."""

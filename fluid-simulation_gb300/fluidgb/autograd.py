@@ -2,12 +2,14 @@
 fl_step_adjoint), wrapped in a torch.autograd.Function.
 
 The forward pass runs `steps` substeps and keeps a checkpoint (particles, ids,
-warm-start pressure: fl_save_state) every `checkpoint_every` substeps.  The
-backward pass walks the segments in reverse: it restores a segment's
-checkpoint, recomputes the segment while recording a tape (the recomputation
-is bit-identical to the forward), then pops the tape step by step through the
-adjoint kernels.  Memory: one tape of `checkpoint_every` substeps plus the
-checkpoints.
+warm-start pressure: fl_save_state_device) every `checkpoint_every`
+substeps, in device memory; it records the last segment on the tape as it
+goes.  The backward pass walks the segments in reverse: the last one is popped
+straight from the tape; every earlier one is restored from its checkpoint and
+recomputed while recording (the recomputation is bit-identical to the
+forward), then popped step by step through the adjoint kernels.  Memory: one
+tape of `checkpoint_every` substeps plus the checkpoints; nothing leaves the
+GPU.  With checkpoint_every >= steps nothing is recomputed.
 
 Gradients are taken with respect to the initial per-particle state and the
 gravity (body-force) vector, as in the differentiable-rollout workload:
@@ -19,9 +21,26 @@ import torch
 from ._abi import Fluid
 
 
+def _as_device_particles(particles, dev):
+    if isinstance(particles, torch.Tensor):
+        t = particles.detach().to(device=dev, dtype=torch.float32)
+    else:
+        t = torch.from_numpy(np.ascontiguousarray(particles, np.float32)).to(dev)
+    if t.dim() != 2 or t.shape[1] != 8:
+        raise ValueError("particles must be (N, 8) float32: pos.xyz, pad, vel.xyz, pad")
+    return t.contiguous()
+
+
 class Rollout:
+    """A checkpointed rollout of one handle.  All buffers live on the current
+    CUDA device; the handle runs on a stream of its own, ordered against the
+    caller's stream at entry and exit."""
+
     def __init__(self, params, capacity, steps, checkpoint_every=10, adj_cg_iters=1000, adj_cg_tol=1e-6):
+        self.dev = torch.device("cuda", torch.cuda.current_device())
+        self.stream = torch.cuda.Stream(self.dev)
         self.fluid = Fluid(params, capacity)
+        self.fluid.set_stream(self.stream.cuda_stream)
         self.params = params.copy()
         self.steps = int(steps)
         self.k = max(1, int(checkpoint_every))
@@ -29,73 +48,110 @@ class Rollout:
         self.adj_cg_tol = adj_cg_tol
         self.tape = self.fluid.tape(self.k)
         self.checkpoints = {}
+        self.taped = None
+        self.n = 0
+        self.adj_cg_iterations = []
 
     def close(self):
         self.tape.close()
         self.fluid.close()
 
-    def forward(self, particles0, gravity):
-        """particles0: (N, 8) float32 array (input order).  Returns the final
-        particles (N, 8) and their ids (input slots)."""
+    def _enter(self):
+        self.stream.wait_stream(torch.cuda.current_stream(self.dev))
+        return torch.cuda.stream(self.stream)
+
+    def _leave(self):
+        torch.cuda.current_stream(self.dev).wait_stream(self.stream)
+
+    def set_gravity(self, gravity):
         p = self.params.copy()
         p.grav[0], p.grav[1], p.grav[2] = (float(g) for g in gravity)
         p.phys[0] = p.grav[1]
         self.fluid.set_params(p)
-        self.fluid.set_particles(np.ascontiguousarray(particles0, np.float32))
-        self.checkpoints = {}
-        for s in range(self.steps):
-            if s % self.k == 0:
-                self.checkpoints[s] = self.fluid.save_state()
-            self.fluid.step(1)
-        return self.fluid.get_particles()
 
-    def backward(self, g_final, final_ids):
-        """g_final: dL/d(final particles) (N, 8) in the order returned by
-        forward.  Returns dL/d(particles0) (N, 8) in input order and dL/dgravity."""
-        dev = torch.device("cuda")
-        g_out = torch.from_numpy(np.ascontiguousarray(g_final, np.float32)).to(dev)
-        g_in = torch.empty_like(g_out)
-        g_grav = np.zeros(3, np.float64)
-        starts = sorted(self.checkpoints)
-        for s0 in reversed(starts):
-            s1 = min(s0 + self.k, self.steps)
-            self.fluid.load_state(self.checkpoints[s0])
+    def forward(self, particles0, gravity):
+        """particles0: (N, 8) float32 (torch tensor or numpy), input order.
+        Returns the final particles (N, 8) and their ids (input slots, int64),
+        both CUDA tensors."""
+        with self._enter():
+            parts = _as_device_particles(particles0, self.dev)
+            self.n = parts.shape[0]
+            self.set_gravity(gravity)
+            self.fluid.set_particles_device(parts.data_ptr(), self.n)
+            size = self.fluid.state_size()
+            last = ((self.steps - 1) // self.k) * self.k if self.steps else 0
             self.tape.clear()
-            for _ in range(s0, s1):
-                self.tape.record()
-            torch.cuda.synchronize()
-            for _ in range(s0, s1):
-                gg = self.tape.adjoint(g_out.data_ptr(), g_in.data_ptr(), self.adj_cg_iters, self.adj_cg_tol)
-                g_grav += np.asarray(gg, np.float64)
-                g_out, g_in = g_in, g_out
-        return g_out.cpu().numpy(), g_grav
+            for s in range(self.steps):
+                if s % self.k == 0:
+                    buf = self.checkpoints.get(s)
+                    if buf is None or buf.numel() != size:
+                        buf = torch.empty(size, dtype=torch.uint8, device=self.dev)
+                        self.checkpoints[s] = buf
+                    self.fluid.save_state_device(buf.data_ptr(), size)
+                if s >= last:
+                    self.tape.record()
+                else:
+                    self.fluid.step(1)
+            self.taped = last
+            for s in [s for s in self.checkpoints if s >= self.steps or s % self.k]:
+                del self.checkpoints[s]
+            final = torch.empty((self.n, 8), dtype=torch.float32, device=self.dev)
+            ids = torch.empty(self.n, dtype=torch.int32, device=self.dev)
+            self.fluid.get_particles_device(final.data_ptr(), ids.data_ptr())
+        self._leave()
+        return final, ids.long()
+
+    def backward(self, g_final):
+        """g_final: dL/d(final particles) (N, 8) in the order forward returned
+        them.  Returns dL/d(particles0) (N, 8, CUDA tensor, input order) and
+        dL/dgravity (3 doubles)."""
+        g_grav = np.zeros(3, np.float64)
+        self.adj_cg_iterations = []
+        with self._enter():
+            g_out = _as_device_particles(g_final, self.dev).clone()
+            g_in = torch.empty_like(g_out)
+            for s0 in sorted(self.checkpoints, reverse=True):
+                s1 = min(s0 + self.k, self.steps)
+                if s0 != self.taped or len(self.tape) != s1 - s0:
+                    buf = self.checkpoints[s0]
+                    self.fluid.load_state_device(buf.data_ptr(), buf.numel())
+                    self.tape.clear()
+                    for _ in range(s0, s1):
+                        self.tape.record()
+                self.taped = None
+                for _ in range(s0, s1):
+                    gg = self.tape.adjoint(g_out.data_ptr(), g_in.data_ptr(), self.adj_cg_iters, self.adj_cg_tol)
+                    self.adj_cg_iterations.append(self.tape.last_stats()["cg_iterations"])
+                    g_grav += np.asarray(gg, np.float64)
+                    g_out, g_in = g_in, g_out
+        self._leave()
+        return g_out, g_grav
 
 
 class RolloutFunction(torch.autograd.Function):
     """(initial velocity (N,3), gravity (3,)) -> final positions (N,3), rows by
-    particle id.  Initial positions are fixed (ctx input)."""
+    particle id.  Initial positions are fixed (ctx input).  Device-resident."""
 
     @staticmethod
     def forward(ctx, vel0, gravity, pos0, rollout):
         n = pos0.shape[0]
-        parts = np.zeros((n, 8), np.float32)
-        parts[:, 0:3] = pos0.detach().cpu().numpy()
-        parts[:, 4:7] = vel0.detach().cpu().numpy()
+        parts = torch.zeros((n, 8), dtype=torch.float32, device=vel0.device)
+        parts[:, 0:3] = pos0.detach()
+        parts[:, 4:7] = vel0.detach()
         final, ids = rollout.forward(parts, gravity.detach().cpu().numpy())
         ctx.rollout = rollout
-        ctx.ids = ids
-        out = np.empty((n, 3), np.float32)
+        ctx.save_for_backward(ids)
+        out = torch.empty((n, 3), dtype=torch.float32, device=vel0.device)
         out[ids] = final[:, 0:3]
-        return torch.from_numpy(out).to(vel0.device)
+        return out
 
     @staticmethod
     def backward(ctx, g_pos):
-        ids = ctx.ids
-        g = g_pos.detach().cpu().numpy()
-        gf = np.zeros((ids.size, 8), np.float32)
-        gf[:, 0:3] = g[ids]
-        g0, g_grav = ctx.rollout.backward(gf, ids)
-        dvel = torch.from_numpy(np.ascontiguousarray(g0[:, 4:7])).to(g_pos.device)
+        (ids,) = ctx.saved_tensors
+        gf = torch.zeros((ids.numel(), 8), dtype=torch.float32, device=g_pos.device)
+        gf[:, 0:3] = g_pos[ids]
+        g0, g_grav = ctx.rollout.backward(gf)
+        dvel = g0[:, 4:7].contiguous()
         dgrav = torch.tensor(g_grav, dtype=g_pos.dtype, device=g_pos.device)
         return dvel, dgrav, None, None
 

@@ -173,30 +173,42 @@ fl_status fl_save_state(fl_handle* h, void* buf, size_t* size_inout);
 fl_status fl_load_state(fl_handle* h, const void* buf, size_t size);
 
 /* Device-buffer particle copies (8 floats per particle, 16-byte aligned):
- * out of the handle (n = fl_particle_count), and into it (n <= capacity; the
- * warm-start pressure and the reset copy are kept). */
-fl_status fl_get_particles_device(fl_handle* h, void* dst_dev);
+ * out of the handle (n = fl_particle_count particles and, if ids_dev is not
+ * NULL, their ids as fl_get_particles gives them), and into it (n <= capacity;
+ * ids become the input slots 0..n-1; the warm-start pressure and the reset
+ * copy are kept).  No reference counterpart: the reference's particles live
+ * in its own GPU buffers (fluid.rs), which these stand in for. */
+fl_status fl_get_particles_device(fl_handle* h, void* dst_dev, uint32_t* ids_dev);
 fl_status fl_set_particles_device(fl_handle* h, const void* src_dev, uint32_t n);
+
+/* fl_save_state / fl_load_state with the blob in device memory (same layout
+ * and size; 256-byte aligned buffer): checkpoints of a rollout stay in HBM. */
+fl_status fl_save_state_device(fl_handle* h, void* dst_dev, size_t* size_inout);
+fl_status fl_load_state_device(fl_handle* h, const void* src_dev, size_t size);
 
 /* ---- adjoint (differentiable rollout) ----
  * A tape records the forward intermediates of up to `max_steps` substeps:
- * bin-ordered particles, the bin permutation, cell types, the fixed-point P2G
- * weights, the saved and the final face velocities (36 B per particle and
- * C + 12 B per face, per step).  fl_step_record runs one substep like
+ * bin-ordered particles, the bin permutation, cell types, the saved and the
+ * final face velocities (36 B per particle, 1 B per cell and 8 B per face,
+ * per step).  fl_step_record runs one substep like
  * fl_step(h, 1) and appends it.  fl_step_adjoint pops the last recorded step:
  * given dL/d(particles after the step) — 8 floats per particle, in the order
  * fl_get_particles returns after that step — it writes dL/d(particles before
  * the step) in the order they had before it, and adds dL/d(gravity vector) to
  * dL_dgrav[3].  Discrete choices (bins, cell types, clamps) are held fixed;
+ * the fixed-point P2G normalisation is linearised at its unquantised sums;
  * the pressure solve is differentiated as an exact solve, so the adjoint runs
- * a second CG (FP64 reductions) with the same operator, to `adj_cg_tol`
+ * a second CG with the same operator and the handle's cg_precision, to `adj_cg_tol`
  * relative residual or `adj_cg_iters` iterations.  Requires advect_order 1
- * and wall_friction 0.  Gradient buffers are device pointers. */
+ * and wall_friction 0.  Gradient buffers are device pointers.
+ * fl_tape_last_stats: cg_iterations, rs_initial/rs_final and device_status of
+ * the last adjoint pressure solve. */
 typedef struct fl_tape fl_tape;
 fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out);
 fl_status fl_tape_free(fl_tape* t);
 fl_status fl_tape_clear(fl_tape* t);
 fl_status fl_tape_count(const fl_tape* t, uint32_t* n_out);
+fl_status fl_tape_last_stats(const fl_tape* t, fl_stats* out);
 fl_status fl_step_record(fl_handle* h, fl_tape* t);
 fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, void* dL_din_dev, float* dL_dgrav,
                           uint32_t adj_cg_iters, float adj_cg_tol);

@@ -111,10 +111,15 @@ def test_checkpointed_recompute_matches_forward():
     p, parts, steps = setup_case(steps=5)
     roll = Rollout(p, parts.shape[0], steps, checkpoint_every=2)
     final, ids = roll.forward(parts, (0.0, -9.81, 0.0))
-    roll.fluid.load_state(roll.checkpoints[4])
+    assert sorted(roll.checkpoints) == [0, 2, 4]
+    buf = roll.checkpoints[4]
+    roll.fluid.load_state_device(buf.data_ptr(), buf.numel())
     roll.fluid.step(1)
     again, ids2 = roll.fluid.get_particles()
-    assert np.array_equal(final, again) and np.array_equal(ids, ids2)
+    assert np.array_equal(final.cpu().numpy(), again) and np.array_equal(ids.cpu().numpy(), ids2)
+    # the device checkpoint holds the same bytes as the host one
+    roll.fluid.load_state_device(buf.data_ptr(), buf.numel())
+    assert roll.fluid.save_state() == bytes(buf.cpu().numpy())
     roll.close()
 
 
@@ -130,10 +135,11 @@ def test_adjoint_position_and_chain_diagnostics(oracle, steps, k, what):
     n = parts.shape[0]
     roll = Rollout(p, n, steps, checkpoint_every=k, adj_cg_iters=3000, adj_cg_tol=1e-7)
     final, ids = roll.forward(parts, (0.0, np.float32(-9.81), 0.0))
-    c = final[:, 0:3].astype(np.float64).mean(axis=0)
+    c = final[:, 0:3].cpu().numpy().astype(np.float64).mean(axis=0)
     g = np.zeros((n, 8), np.float32)
     g[:, 0:3] = (2.0 * (c - TARGET) / n).astype(np.float32)
-    g0, g_grav = roll.backward(g, ids)
+    g0, g_grav = roll.backward(g)
+    g0 = g0.cpu().numpy()
     roll.close()
     oracle.set_exact_p2g(True)
     try:

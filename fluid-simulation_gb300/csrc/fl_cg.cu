@@ -4,444 +4,700 @@
 // 9 dispatches per iteration (fluid.rs:1689-1701): cg_spmv, cg_reduce(d,q),
 // cg_alpha, cg_update, cg_reduce(r,r), cg_beta, cg_dir.  Per iteration:
 //
-//   phase 1  d_new = r + beta*d_old (cg_dir.wgsl:30) fused with q = A d_new
-//            (cg_spmv.wgsl:46-68); neighbours' d_new are recomputed from r and
-//            d_old (same f32 ops, same bits), so no barrier is needed between
-//            the direction update and the stencil.  d ping-pongs between two
-//            buffers.  Partial d.q per 256-cell chunk.
-//   barrier  alpha = rs_old/dq (cg_alpha.wgsl)
-//   phase 2  p += alpha d, r -= alpha q (cg_update.wgsl); partial r.r
-//   barrier  beta, convergence test (cg_beta.wgsl) — the loop really exits.
+//   phase 1   d_new = r + beta*d_old (cg_dir.wgsl:30) fused with q = A d_new
+//             (cg_spmv.wgsl:46-68); neighbours' d_new are recomputed from r and
+//             d_old (same f32 ops, same bits), so no grid-wide step separates
+//             the direction update from the stencil.  d ping-pongs between two
+//             buffers.  One d.q partial per 256-cell chunk.
+//   exchange  alpha = rs_old/dq (cg_alpha.wgsl)
+//   phase 2   p += alpha d, r -= alpha q (cg_update.wgsl); r.r partials
+//   exchange  beta and the convergence test (cg_beta.wgsl); the loop exits.
+//
+// Exchange = grid barrier and reduction in one step.  Every partial is
+// published as one 64-bit word {tag, value} with a release store; each block
+// polls all partials with acquire loads until every word carries the
+// exchange's tag, then reduces them itself.  No counter, no second read of
+// the partials, no broadcast: seeing the tags is the barrier, and all blocks
+// evaluate the same reduction in the same order.  Tags are unique per solve
+// (a per-area epoch advanced by k_cg_plan), so words left by earlier solves
+// never match.  A block's release covers all of its vector writes of the
+// phase, which is what the next phase's neighbour loads need.
 //
 // Only 256-cell chunks holding a liquid cell are visited (the rest are zero in
 // every vector).  k_cg_plan lists them once per solve, grouped by residue
 // chunk mod 256 and ascending within a group: segment li holds exactly the
 // nonzero terms that thread li of cg_reduce_final.wgsl adds in sequence (the
 // skipped terms are +0, and acc + 0 == acc for an accumulator that starts at
-// +0).  Partials are stored in plan order, so in FL_CG_F32 every block
-// re-evaluates the reference's two-level tree from contiguous segments; all
-// blocks hold identical scalars without a broadcast and the result is the
-// reference's f32 arithmetic exactly.  Each group caches its plan entries and
-// a list of its liquid cells with their stencil masks (k_grid_prep's cinfo) in
-// shared memory for the whole solve: an iteration touches liquid cells only,
-// issues no dependent loads for topology, scatters each product into its fixed
-// slot of the chunk's tree, and reduces KB chunks at a time with one
-// multi-tree.  FL_CG_F64: see Df below.
+// +0).  It also splits the plan into one contiguous range per block with equal
+// liquid-cell weight.  FL_CG_F32: a warp evaluates a chunk's 256-wide
+// cg_reduce.wgsl tree (same pairing, same order); every block stages all chunk
+// partials, sums its segments and evaluates the cg_reduce_final.wgsl tree, so
+// the scalars are the reference's f32 arithmetic exactly.  FL_CG_F64: see Df.
+// Each block lists its liquid cells with their stencil masks (k_grid_prep's
+// cinfo) in shared memory once per solve; an iteration then touches liquid
+// cells only and issues no dependent loads for topology.
 #include "fl_device.cuh"
 
 namespace fl {
 
-constexpr int KPLAN = 64;  // plan entries cached in shared memory per group
-constexpr int KINFO = 24;  // chunks per group whose liquid cells are listed in shared memory
-constexpr int KB = 4;      // chunks reduced together by one multi-tree
-constexpr int NBATCH = KINFO / KB;
-constexpr int KCELL = KINFO * CHUNK;  // listed cells per group
+constexpr int CG_WARPS = CG_THREADS / 32;
+constexpr uint32_t KT = CG_WARPS;        // chunks per tree pass: one chunk tree per warp
+constexpr uint32_t CELL_CAP = 16384;     // liquid cells listed per block
+constexpr uint32_t KCH = 2048;           // chunk ids cached per block
+constexpr uint32_t VAL_CAP = 20480;      // chunk partials staged per window
+constexpr uint32_t MAX_PASS = KCH / KT;  // cached tree passes
+constexpr uint32_t TAG_SPAN_MAX = 1u << 30;
+constexpr int STAGE_BATCH = 4;
+constexpr uint32_t MAX_CG_BLOCKS = 1024;
 
 struct CgShared {
-    uint32_t off[CHUNK + 1];
-    uint32_t plan[CG_GROUPS][KPLAN];
-    float tree[CG_GROUPS][KB][CHUNK];
-    // Liquid cells of the group's first KINFO chunks, grouped by batch of KB
-    // chunks: bits 0-9 stencil mask (cinfo), 10-17 cell in chunk, 18-23 chunk slot.
-    uint32_t cell[CG_GROUPS][KCELL];
-    uint32_t boff[CG_GROUPS][NBATCH + 1];
-    uint32_t wcnt[CG_GROUPS][KINFO][CHUNK / 32];  // per (chunk slot, warp): count, then list offset
-    double red64[CG_THREADS / 32];
-    float scal_f;
-    double scal_d;
-    int abort_flag;
+    float tree[KT][CHUNK];     // per-chunk products of one pass, tree slot = cell in chunk
+    float vals[VAL_CAP];       // staged partials of one exchange window
+    uint32_t cell[CELL_CAP];   // listed liquid cells: bits 0-9 stencil mask, 10-17 cell in chunk, 18-31 chunk
+    uint32_t chunk[KCH];       // this block's chunk ids (plan order)
+    uint32_t off[CHUNK + 1];   // plan segment offsets
+    uint32_t pass_off[MAX_PASS + 1];
+    float seg[CHUNK];          // segment sums (cg_reduce_final.wgsl thread accumulators)
+    float red[2 * CG_WARPS];   // float-float warp partials
+    uint32_t wcnt[CG_WARPS];
+    uint32_t bstart[MAX_CG_BLOCKS + 1];  // first plan entry of every block
 };
 
-__device__ __forceinline__ void named_bar(int id, int count) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
-}
+// ---------------------------------------------------------------------------
+// Tagged words
 
-// cg_reduce.wgsl:38-49 over the 256 threads of one group.  Valid at lt == 0.
-__device__ __forceinline__ float group_tree(float prod, float* s, int group, int lt) {
-    s[lt] = prod;
-    named_bar(1 + group, CHUNK);
-    if (lt < 128) s[lt] = __fadd_rn(s[lt], s[lt + 128]);
-    named_bar(1 + group, CHUNK);
-    if (lt < 64) s[lt] = __fadd_rn(s[lt], s[lt + 64]);
-    named_bar(1 + group, CHUNK);
-    float v = 0.0f;
-    if (lt < 32) {
-        v = __fadd_rn(s[lt], s[lt + 32]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
-    }
-    named_bar(1 + group, CHUNK);  // s is reused afterwards
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-
-// The same tree over nb <= KB arrays at once (one barrier per level for all
-// of them); warp w of the group finishes array w with shuffles and writes its
-// partial to out[e0 + w*estride].
-__device__ __forceinline__ void multi_tree(float (*s)[CHUNK], uint32_t nb, int group, int lt, float* out,
-                                           uint32_t e0, uint32_t estride) {
-    named_bar(1 + group, CHUNK);
-    if (lt < 128)
-        for (uint32_t k = 0; k < nb; k++) s[k][lt] = __fadd_rn(s[k][lt], s[k][lt + 128]);
-    named_bar(1 + group, CHUNK);
-    if (lt < 64)
-        for (uint32_t k = 0; k < nb; k++) s[k][lt] = __fadd_rn(s[k][lt], s[k][lt + 64]);
-    named_bar(1 + group, CHUNK);
-    const uint32_t w = (uint32_t)lt >> 5, lane = (uint32_t)lt & 31u;
-    if (w < nb) {
-        float v = __fadd_rn(s[w][lane], s[w][lane + 32]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
-        if (lane == 0) out[e0 + w * estride] = v;
-    }
-    named_bar(1 + group, CHUNK);
+__device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
-
-// cg_reduce_final.wgsl:24-53: thread li sums the nonzero partials of chunks
-// li, li+256, ... in order (its plan segment), then the 256-wide tree.
-// Evaluated by group 0; the result goes to all threads.  With `chunk_ids`, the
-// partials are indexed by chunk (the initial residual from k_grid_prep); else
-// they are stored in plan order.
-__device__ float final_reduce_f32(const float* part, const uint32_t* chunk_ids, CgShared& sh) {
-    __syncthreads();
-    if (threadIdx.x < CHUNK) {
-        float acc = 0.0f;
-        const uint32_t beg = sh.off[threadIdx.x], end = sh.off[threadIdx.x + 1];
-        if (chunk_ids) {
-            for (uint32_t e = beg; e < end; e++) acc = __fadd_rn(acc, part[chunk_ids[e]]);
-        } else {
-#pragma unroll 4
-            for (uint32_t e = beg; e < end; e++) acc = __fadd_rn(acc, part[e]);
-        }
-        const float v = group_tree(acc, sh.tree[0][0], 0, threadIdx.x);
-        if (threadIdx.x == 0) sh.scal_f = v;
-    }
-    __syncthreads();
-    return sh.scal_f;
-}
-
-// Deterministic f64 sum of n values (lanes stride, then a fixed shuffle tree);
-// with `ids`, value i is part[ids[i]].
-__device__ double final_reduce_f64(const double* part, uint32_t n, CgShared& sh, const uint32_t* ids = nullptr) {
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        double acc = 0.0;
-        for (uint32_t i = threadIdx.x; i < n; i += 32) acc += part[ids ? ids[i] : i];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (threadIdx.x == 0) sh.scal_d = acc;
-    }
-    __syncthreads();
-    return sh.scal_d;
-}
-
-// FL_CG_F64 accumulation: exact f32 products (two-product with fmaf) summed in
-// compensated float-float (two-sum) by each thread and across its warp, then
-// in double across warps, blocks and the grid.  The FP64 pipe of this part is
-// slow, so it is used where the error would otherwise grow: the ~1e5-term sums
-// across warps/blocks, alpha, beta, the residual norm and the stopping test.
-struct Df {
-    float hi, lo;
-};
-__device__ __forceinline__ Df df_add(Df a, Df b) {
-    const float s = __fadd_rn(a.hi, b.hi);
-    const float bb = __fsub_rn(s, a.hi);
-    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
-    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
-    const float hi = __fadd_rn(s, e);
-    return {hi, __fsub_rn(e, __fsub_rn(hi, s))};
-}
-__device__ __forceinline__ Df df_prod(float x, float y) {
-    const float p = __fmul_rn(x, y);
-    return {p, __fmaf_rn(x, y, -p)};
-}
-
-__device__ __forceinline__ Df warp_sum_df(Df v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        Df w;
-        w.hi = __shfl_down_sync(0xffffffffu, v.hi, o);
-        w.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
-        v = df_add(v, w);
-    }
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
 }
-
-// Block partial: float-float across lanes and then across the block's warps
-// (in warp order), one conversion to double at the end.
-__device__ void block_sum_df(Df v, double* out, CgShared& sh) {
-    v = warp_sum_df(v);
-    float* red = reinterpret_cast<float*>(sh.red64);
-    if ((threadIdx.x & 31) == 0) {
-        red[2 * (threadIdx.x >> 5)] = v.hi;
-        red[2 * (threadIdx.x >> 5) + 1] = v.lo;
-    }
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        Df w = {red[2 * threadIdx.x], red[2 * threadIdx.x + 1]};
-        w = warp_sum_df(w);
-        if (threadIdx.x == 0) *out = (double)w.hi + (double)w.lo;
-    }
+// `rel`: release store, for the exchange after which other blocks read this
+// block's vector writes; the other exchange carries only its partials.
+__device__ __forceinline__ void publish(unsigned long long* p, uint32_t tag, float v, bool rel) {
+    const unsigned long long w = ((unsigned long long)tag << 32) | (unsigned long long)__float_as_uint(v);
+    if (rel) st_release_u64(p, w);
+    else st_relaxed_u64(p, w);
+}
+__device__ __forceinline__ unsigned long long ld_tag(const unsigned long long* p, bool acq) {
+    return acq ? ld_acquire_u64(p) : ld_relaxed_u64(p);
 }
 
-// Grid barrier with a bounded wait (see fl_device.cuh).  false = abort.
-__device__ bool grid_barrier(DevStats* st, uint32_t target, CgShared& sh) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        red_release_add(&st->barrier, 1u);
-        const uint64_t t0 = global_ns();
-        int ab = 0;
-        uint32_t spins = 0;
-        while (ld_acquire(&st->barrier) < target) {
-            if ((++spins & 255u) != 0u) continue;  // poll the counter; check the rest now and then
-            if (*(volatile uint32_t*)&st->status != 0u) { ab = 1; break; }
+// Polls *p until it carries `tag` and returns the word.  Bounded: after about
+// 2 s, or once another block recorded an error, it records FL_TIMEOUT and
+// returns a word without the tag.
+__device__ __noinline__ unsigned long long wait_tag(const unsigned long long* p, uint32_t tag, DevStats* st, bool acq) {
+    const uint64_t t0 = global_ns();
+    uint32_t spins = 0;
+    unsigned long long w = ld_tag(p, acq);
+    while ((uint32_t)(w >> 32) != tag) {
+        if ((++spins & 63u) == 0u) {
+            if (*(volatile uint32_t*)&st->status != 0u) return 0ull;
             if (global_ns() - t0 > 2000000000ull) {
                 atomicCAS(&st->status, 0u, 5u /* FL_TIMEOUT */);
-                ab = 1;
-                break;
+                return 0ull;
             }
         }
-        sh.abort_flag = ab;
+        w = ld_tag(p, acq);
     }
-    __syncthreads();
-    return sh.abort_flag == 0;
+    return w;
 }
 
-// The solve's plan: active chunks grouped by residue mod 256 (one block).
-__global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b) {
-    __shared__ uint32_t s_warp[CHUNK / 32];
-    const uint32_t nchunks = b.prm->nchunks;
+// Stages words x[e0 + i*stride(i)] for i < n (all carrying `tag`) into vals[i]:
+// STAGE_BATCH loads in flight per thread.  Word i sits at (i / per) * 16 + i % per
+// when per != 0 (`per` words of each block on their own 128-byte line), else
+// at e0 + i.  Returns false on abort.
+__device__ __forceinline__ bool stage_tagged(const unsigned long long* x, uint32_t e0, uint32_t n, uint32_t tag,
+                                             float* vals, DevStats* st, bool acq, uint32_t per = 0) {
+    bool ok = true;
+    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += STAGE_BATCH * CG_THREADS) {
+        unsigned long long w[STAGE_BATCH];
+#pragma unroll
+        for (int k = 0; k < STAGE_BATCH; k++) {
+            const uint32_t i = i0 + k * CG_THREADS;
+            const uint32_t at = per ? (i / per) * 16u + i % per : e0 + i;
+            w[k] = i < n ? ld_tag(x + at, acq) : 0ull;
+        }
+#pragma unroll
+        for (int k = 0; k < STAGE_BATCH; k++) {
+            const uint32_t i = i0 + k * CG_THREADS;
+            if (i < n && ok) {
+                if ((uint32_t)(w[k] >> 32) != tag) {
+                    const uint32_t at = per ? (i / per) * 16u + i % per : e0 + i;
+                    w[k] = wait_tag(x + at, tag, st, acq);
+                    ok = (uint32_t)(w[k] >> 32) == tag;
+                }
+                vals[i] = __uint_as_float((uint32_t)w[k]);
+            }
+        }
+    }
+    return ok;
+}
+
+// ---------------------------------------------------------------------------
+// Reductions
+
+// cg_reduce.wgsl:38-49 over s[0..255], evaluated by one warp: lane l forms the
+// level-128 sums of indices l, l+32, l+64, l+96, the level-64 sums of l and
+// l+32, the level-32 sum of l, then the same shuffle steps 16..1.  Operand
+// order and pairing equal the 256-thread tree's.  Valid in lane 0.
+__device__ __forceinline__ float chunk_tree(const float* s, uint32_t lane) {
+    const float a0 = __fadd_rn(s[lane], s[lane + 128]);
+    const float a1 = __fadd_rn(s[lane + 32], s[lane + 160]);
+    const float a2 = __fadd_rn(s[lane + 64], s[lane + 192]);
+    const float a3 = __fadd_rn(s[lane + 96], s[lane + 224]);
+    float v = __fadd_rn(__fadd_rn(a0, a2), __fadd_rn(a1, a3));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// FL_CG_F64: inner products accumulated in float-float (fl_device.cuh) by each
+// thread, across its block and across blocks; alpha and beta are float-float
+// quotients rounded to f32, and the stopping test compares float-float values.
+
+// a / b rounded to f32: the f32 quotient plus one float-float correction.
+__device__ __forceinline__ float df_div(Df a, Df b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float p = __fmul_rn(q1, b.hi);
+    const float pe = __fmaf_rn(q1, b.hi, -p);  // q1*b.hi - p, exact
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), __fmul_rn(q1, b.lo)), a.lo);
+    return __fadd_rn(q1, __fdiv_rn(r, b.hi));
+}
+__device__ __forceinline__ bool df_le(Df a, Df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+__device__ __forceinline__ double df_to_double(Df a) { return (double)a.hi + (double)a.lo; }
+
+// ---------------------------------------------------------------------------
+// Plan
+
+// One block of 256 threads.  Lists the active chunks by residue (segment li =
+// chunks li, li+256, ... ascending), splits the list into G contiguous ranges
+// of equal weight (liquid cells + 32 per chunk), and reserves this solve's
+// tag range.  When the 32-bit epoch would wrap, the exchange words are
+// cleared first, so no stale word can carry a tag of a later solve.
+__global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
+    __shared__ uint32_t s_wc[CHUNK / 32], s_ww[CHUNK / 32];
+    __shared__ int s_wrap;
+    const DevParams& P = *b.prm;
+    const uint32_t nchunks = P.nchunks;
     const uint32_t li = threadIdx.x, lane = li & 31, warp = li >> 5;
-    uint32_t cnt = 0;
-    for (uint32_t c = li; c < nchunks; c += CHUNK) cnt += b.chunk_flag[c] ? 1u : 0u;
-    uint32_t x = cnt;
+    uint32_t* hdr = b.cg_off;
+    uint32_t* start = hdr + CHUNK + 3;
+    uint32_t cnt = 0, wsum = 0;
+    for (uint32_t c = li; c < nchunks; c += CHUNK) {
+        const uint32_t f = b.chunk_flag[c];
+        if (f) {
+            cnt++;
+            wsum += f + 32u;
+        }
+    }
+    uint32_t x = cnt, y = wsum;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= (uint32_t)o) x += y;
+        const uint32_t xa = __shfl_up_sync(0xffffffffu, x, o), ya = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= (uint32_t)o) {
+            x += xa;
+            y += ya;
+        }
     }
-    if (lane == 31) s_warp[warp] = x;
+    if (lane == 31) {
+        s_wc[warp] = x;
+        s_ww[warp] = y;
+    }
     __syncthreads();
-    uint32_t base = 0;
-    for (uint32_t w = 0; w < warp; w++) base += s_warp[w];
+    uint32_t base = 0, wbase = 0, A = 0, W = 0;
+    for (uint32_t w = 0; w < CHUNK / 32; w++) {
+        if (w < warp) {
+            base += s_wc[w];
+            wbase += s_ww[w];
+        }
+        A += s_wc[w];
+        W += s_ww[w];
+    }
     const uint32_t off = base + x - cnt;
-    b.cg_off[li] = off;
-    if (li == CHUNK - 1) b.cg_off[CHUNK] = off + cnt;
+    hdr[li] = off;
+    if (li == CHUNK - 1) hdr[CHUNK] = off + cnt;
     uint32_t pos = off;
-    for (uint32_t c = li; c < nchunks; c += CHUNK)
-        if (b.chunk_flag[c]) b.cg_chunk[pos++] = c;
+    uint64_t X = wbase + y - wsum;  // weight of all plan entries before `pos`
+    for (uint32_t c = li; c < nchunks; c += CHUNK) {
+        const uint32_t f = b.chunk_flag[c];
+        if (!f) continue;
+        b.cg_chunk[pos] = c;
+        const uint64_t X1 = X + f + 32u;
+        // blocks bb with X*G < bb*W <= X1*G start after this entry
+        const uint64_t lo = X * G / W + 1, hi = X1 * G / W;
+        for (uint64_t bb = lo; bb <= hi; bb++) start[bb] = pos + 1;
+        X = X1;
+        pos++;
+    }
+    if (A == 0)
+        for (uint32_t bb = li; bb <= G; bb += CHUNK) start[bb] = 0;
+    else if (li == 0)
+        start[0] = 0;
+    __syncthreads();
+    // Slot layout: block bb's chunk partials at bb*S + j when every block's
+    // range fits S (a multiple of 16 words, so each block starts a 128-byte
+    // line) and the area holds G*S words; else densely at plan entry s_bb + j.
+    uint32_t mmax = 0;
+    for (uint32_t bb = li; bb < G; bb += CHUNK) {
+        const uint32_t mb = start[bb + 1] - start[bb];
+        mmax = mb > mmax ? mb : mmax;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const uint32_t v = __shfl_xor_sync(0xffffffffu, mmax, o);
+        mmax = v > mmax ? v : mmax;
+    }
+    if (lane == 0) s_wc[warp] = mmax;
+    __syncthreads();
+    if (li == 0) {
+        for (uint32_t w = 0; w < CHUNK / 32; w++) mmax = s_wc[w] > mmax ? s_wc[w] : mmax;
+        const uint64_t S = (mmax + 15u) & ~15u;
+        hdr[CHUNK + 2] = (A > 0 && A <= VAL_CAP && S * G <= (uint64_t)nchunks + 16u * G) ? (uint32_t)S : 0u;
+    }
+    if (li == 0) {
+        const uint32_t span = 2u * (P.iters < TAG_SPAN_MAX ? P.iters : TAG_SPAN_MAX) + 4u;
+        uint32_t e0 = (uint32_t)b.cg_x[0];
+        int wrap = 0;
+        if (e0 > 0xffffffffu - span) {
+            wrap = 1;
+            e0 = 0;
+        }
+        b.cg_x[0] = (unsigned long long)(e0 + span);
+        hdr[CHUNK + 1] = e0;
+        s_wrap = wrap;
+    }
+    __syncthreads();
+    if (s_wrap) {
+        const size_t n = cg_x_words(nchunks, G);
+        for (size_t i = 1 + li; i < n; i += CHUNK) b.cg_x[i] = 0ull;
+    }
 }
 
+// ---------------------------------------------------------------------------
+// The solve
+
+template <bool F64>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CgShared& sh = *reinterpret_cast<CgShared*>(smem_raw);
+    // Settings in registers: the L1 is invalidated at every exchange.
     const DevParams& P = *b.prm;
-    const uint32_t C = P.C, iters = P.iters;
-    const size_t nx = P.nx, nxy = (size_t)P.nx * P.ny;
-    const int group = threadIdx.x >> 8, lt = threadIdx.x & (CHUNK - 1);
-    const uint32_t G = gridDim.x;
-    const bool f64 = P.precision == 1u;
+    const uint32_t C = P.C, iters = P.iters < TAG_SPAN_MAX ? P.iters : TAG_SPAN_MAX, nchunks = P.nchunks;
+    const uint32_t nx = P.nx, nxy = P.nx * P.ny;  // grids hold at most 2^30 cells
+    constexpr bool f64 = F64;
+    const float tol_sq = P.tol_sq;
+    const double tol_sq_d = P.tol_sq_d;
+    DevStats* st = b.st;
+    const uint32_t G = gridDim.x, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     float* __restrict__ r = b.r;
     float* __restrict__ p = b.p;
     float* __restrict__ q = b.q;
     const uint16_t* __restrict__ cinfo = b.cinfo;
-    double* cta64 = b.cta_part64;
-    uint32_t target = 0;
-    for (int i = threadIdx.x; i <= CHUNK; i += blockDim.x) sh.off[i] = b.cg_off[i];
-    __syncthreads();
-    const uint32_t A = sh.off[CHUNK];  // active chunks
     const uint32_t* __restrict__ plan = b.cg_chunk;
-    // This group's plan entries are e_j = gid + j*gstride, j < nk.
-    const uint32_t gid = blockIdx.x * CG_GROUPS + group, gstride = G * CG_GROUPS;
-    const uint32_t nk = A > gid ? (A - 1 - gid) / gstride + 1 : 0u;
-    // Cache the entries, and list the liquid cells of the first KINFO chunks
-    // (with their stencil masks) per batch, for the whole solve.
-    const uint32_t lane = (uint32_t)lt & 31u, lt_mask = (1u << lane) - 1u;
-    for (uint32_t j = lt; j < nk && j < (uint32_t)KPLAN; j += CHUNK) sh.plan[group][j] = plan[gid + j * gstride];
-    const uint32_t nkc = nk < (uint32_t)KINFO ? nk : (uint32_t)KINFO;
-    const uint32_t nbt = (nkc + KB - 1) / KB;
-    const uint32_t warp = (uint32_t)lt >> 5;
-    named_bar(1 + group, CHUNK);
-    for (uint32_t j = 0; j < nkc; j++) {
-        const size_t c = (size_t)sh.plan[group][j] * CHUNK + lt;
-        const bool liq = c < C && (cinfo[c] & 1u);
-        const uint32_t m = __ballot_sync(0xffffffffu, liq);
-        if (lane == 0) sh.wcnt[group][j][warp] = (uint32_t)__popc(m);
-    }
-    named_bar(1 + group, CHUNK);
-    if (lt == 0) {  // list order: batch, chunk slot, warp, lane — fixed, so runs repeat bit for bit
-        uint32_t acc = 0;
-        for (uint32_t bt = 0; bt < nbt; bt++) {
-            sh.boff[group][bt] = acc;
-            for (uint32_t j = bt * KB; j < nkc && j < (bt + 1) * KB; j++)
-                for (uint32_t w = 0; w < CHUNK / 32; w++) {
-                    const uint32_t n = sh.wcnt[group][j][w];
-                    sh.wcnt[group][j][w] = acc;
-                    acc += n;
-                }
-        }
-        sh.boff[group][nbt] = acc;
-    }
-    named_bar(1 + group, CHUNK);
-    for (uint32_t j = 0; j < nkc; j++) {
-        const size_t c = (size_t)sh.plan[group][j] * CHUNK + lt;
-        const uint32_t info = c < C ? cinfo[c] : 0u;
-        const bool liq = info & 1u;
-        const uint32_t m = __ballot_sync(0xffffffffu, liq);
-        if (liq) sh.cell[group][sh.wcnt[group][j][warp] + __popc(m & lt_mask)] = (j << 18) | ((uint32_t)lt << 10) | info;
-    }
-    named_bar(1 + group, CHUNK);
+    const uint32_t* hdr = b.cg_off;
+    for (uint32_t i = tid; i <= CHUNK; i += CG_THREADS) sh.off[i] = hdr[i];
+    const uint32_t tag_base = hdr[CHUNK + 1];
+    const uint32_t S = hdr[CHUNK + 2];  // slot line stride per block, 0 = dense plan order
+    const uint32_t* bstart = hdr + CHUNK + 3;
+    for (uint32_t i = tid; i <= G; i += CG_THREADS) sh.bstart[i] = bstart[i];
+    const uint32_t s0 = bstart[blockIdx.x], s1 = bstart[blockIdx.x + 1];
+    const uint32_t m = s1 - s0;  // this block's chunks: plan entries [s0, s1)
+    const uint32_t slot0 = S ? blockIdx.x * S : s0;  // this block's first slot
+    const size_t nslot = (size_t)nchunks + 16 * (size_t)G;
+    unsigned long long* slotA = b.cg_x + 8;        // d.q chunk partials
+    unsigned long long* slotB = slotA + nslot;     // r.r chunk partials
+    unsigned long long* wordA = slotB + nslot;     // FL_CG_F64: {hi, lo} of block b at 16*b
+    unsigned long long* wordB = wordA + 16 * (size_t)G;
+    const uint32_t mch = m < KCH ? m : KCH;
+    for (uint32_t j = tid; j < mch; j += CG_THREADS) sh.chunk[j] = plan[s0 + j];
+    for (uint32_t i = tid; i < KT * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
+    __syncthreads();
+    const uint32_t A = sh.off[CHUNK];
 
+    // List the liquid cells of chunks [0, mc), four chunks per round, in
+    // (chunk, cell) order; stop before CELL_CAP would be exceeded.
+    uint32_t ncell = 0, mc = 0;
+    {
+        const uint32_t lt_mask = (1u << lane) - 1u;
+        for (uint32_t j0 = 0; j0 < mch; j0 += 4) {
+            if ((j0 % KT) == 0 && tid == 0) sh.pass_off[j0 / KT] = ncell;
+            const uint32_t j = j0 + (tid >> 8), cl = tid & (CHUNK - 1);
+            uint32_t info = 0;
+            if (j < mch) {
+                const uint32_t c = sh.chunk[j] * CHUNK + cl;
+                if (c < C) info = cinfo[c];
+            }
+            const bool liq = info & 1u;
+            const uint32_t bal = __ballot_sync(0xffffffffu, liq);
+            if (lane == 0) sh.wcnt[warp] = (uint32_t)__popc(bal);
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+            for (uint32_t w = 0; w < (uint32_t)CG_WARPS; w++) {
+                const uint32_t n = sh.wcnt[w];
+                if (w < warp) before += n;
+                total += n;
+            }
+            __syncthreads();
+            if (ncell + total > CELL_CAP) break;  // uniform: every thread sees the same totals
+            if (liq) sh.cell[ncell + before + __popc(bal & lt_mask)] = info | (cl << 10) | (j << 18);
+            ncell += total;
+            mc = j0 + 4 < mch ? j0 + 4 : mch;
+        }
+    }
+    const uint32_t npc = (mc + KT - 1) / KT;  // cached passes
+    if (tid == 0) sh.pass_off[npc] = ncell;
+    // One pass in all: non-liquid tree slots stay zero for the whole solve.
+    const bool multi = npc > 1 || mc < m;
+    __syncthreads();
+
+    // FL_CG_F32 scalar: the segment sums of cg_reduce_final.wgsl over the
+    // staged partials (windows of VAL_CAP entries, in plan order), then its
+    // 256-wide tree, evaluated by every warp.  `x` == nullptr: the initial
+    // residual partials part_rr, indexed by chunk.  Returns false on abort.
+    auto reduce_f32 = [&](const unsigned long long* x, uint32_t tag, bool acq, float& out) -> bool {
+        float acc = 0.0f;
+        bool ok = true;
+        for (uint32_t w0 = 0; w0 < A; w0 += VAL_CAP) {
+            const uint32_t wn = A - w0 < VAL_CAP ? A - w0 : VAL_CAP;
+            if (x && S) {  // one window (A <= VAL_CAP): walk the blocks' lines
+                for (uint32_t v0 = tid; v0 < G * S; v0 += STAGE_BATCH * CG_THREADS) {
+                    unsigned long long w[STAGE_BATCH];
+                    uint32_t dst[STAGE_BATCH];
+#pragma unroll
+                    for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
+                        const uint32_t v = v0 + k2 * CG_THREADS;
+                        const uint32_t bb = v / S, j = v - bb * S;
+                        const bool use = v < G * S && j < sh.bstart[bb + 1] - sh.bstart[bb];
+                        dst[k2] = use ? sh.bstart[bb] + j : 0xffffffffu;
+                        w[k2] = use ? ld_tag(x + v, acq) : 0ull;
+                    }
+#pragma unroll
+                    for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
+                        if (dst[k2] != 0xffffffffu && ok) {
+                            if ((uint32_t)(w[k2] >> 32) != tag) {
+                                w[k2] = wait_tag(x + v0 + k2 * CG_THREADS, tag, st, acq);
+                                ok = (uint32_t)(w[k2] >> 32) == tag;
+                            }
+                            sh.vals[dst[k2]] = __uint_as_float((uint32_t)w[k2]);
+                        }
+                    }
+                }
+            } else if (x) {
+                ok = stage_tagged(x, w0, wn, tag, sh.vals, st, acq);
+            } else {
+                for (uint32_t i = tid; i < wn; i += CG_THREADS) sh.vals[i] = b.part_rr[plan[w0 + i]];
+            }
+            if (__syncthreads_or(!ok)) return false;
+            if (tid < (uint32_t)CHUNK) {
+                const uint32_t lo = sh.off[tid] > w0 ? sh.off[tid] : w0;
+                const uint32_t hi = sh.off[tid + 1] < w0 + wn ? sh.off[tid + 1] : w0 + wn;
+                uint32_t e = lo;
+                for (; e + 8 <= hi; e += 8) {  // loads first, then the sequential adds
+                    float v[8];
+#pragma unroll
+                    for (int k2 = 0; k2 < 8; k2++) v[k2] = sh.vals[e - w0 + k2];
+#pragma unroll
+                    for (int k2 = 0; k2 < 8; k2++) acc = __fadd_rn(acc, v[k2]);
+                }
+                for (; e < hi; e++) acc = __fadd_rn(acc, sh.vals[e - w0]);
+            }
+            if (w0 + wn < A) __syncthreads();
+        }
+        if (tid < (uint32_t)CHUNK) sh.seg[tid] = acc;
+        __syncthreads();
+        out = __shfl_sync(0xffffffffu, chunk_tree(sh.seg, lane), 0);
+        return true;
+    };
+    // FL_CG_F64 scalar: the blocks' float-float partials (two words of block b
+    // at 16*b), summed by every warp in the same fixed order (lanes stride
+    // over blocks, then a shuffle tree), so no broadcast is needed.
+    auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, Df& out) -> bool {
+        const bool ok = stage_tagged(words, 0, 2 * G, tag, sh.vals, st, acq, 2u);
+        if (__syncthreads_or(!ok)) return false;
+        Df acc = {0.0f, 0.0f};
+        for (uint32_t bb = lane; bb < G; bb += 32) acc = df_add(acc, Df{sh.vals[2 * bb], sh.vals[2 * bb + 1]});
+        out = warp_allsum_df(acc);
+        return true;
+    };
+    // Block float-float partial published as two tagged words on the block's line.
+    auto publish_df = [&](Df acc, unsigned long long* words, uint32_t tag, bool rel) {
+        acc = warp_sum_df(acc);
+        if (lane == 0) {
+            sh.red[2 * warp] = acc.hi;
+            sh.red[2 * warp + 1] = acc.lo;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            Df v = {sh.red[2 * lane], sh.red[2 * lane + 1]};
+            v = warp_sum_df(v);
+            if (lane == 0) {
+                publish(words + 16 * blockIdx.x, tag, v.hi, rel);
+                publish(words + 16 * blockIdx.x + 1, tag, v.lo, rel);
+            }
+        }
+    };
+    // Warp w publishes the tree of chunk j0 + w of the pass.
+    auto publish_trees = [&](uint32_t j0, uint32_t nb, unsigned long long* slots, uint32_t tag, bool rel) {
+        __syncthreads();
+        if (warp < nb) {
+            const float v = chunk_tree(sh.tree[warp], lane);
+            if (lane == 0) publish(slots + slot0 + j0 + warp, tag, v, rel);
+        }
+    };
+
+    // Initial residual norm (cg_init.wgsl + cg_reduce of r.r).
     float rs_old_f = 0.0f, rs_init_f = 0.0f;
-    double rs_old_d = 0.0, rs_init_d = 0.0;
+    Df rs_old_d = {0.0f, 0.0f}, rs_init_d = {0.0f, 0.0f}, thr_d = {0.0f, 0.0f};
     if (f64) {
-        rs_old_d = final_reduce_f64(b.chunk_rr64, A, sh, plan);
-        rs_init_d = rs_old_d;
+        Df acc = {0.0f, 0.0f};
+        for (uint32_t e = tid; e < A; e += CG_THREADS) {
+            const float2 v = b.chunk_rr_df[plan[e]];
+            acc = df_add(acc, Df{v.x, v.y});
+        }
+        acc = warp_allsum_df(acc);
+        if (lane == 0) {
+            sh.red[2 * warp] = acc.hi;
+            sh.red[2 * warp + 1] = acc.lo;
+        }
+        __syncthreads();
+        rs_old_d = rs_init_d = warp_allsum_df(Df{sh.red[2 * lane], sh.red[2 * lane + 1]});
+        // stopping threshold tol^2 * rs_init, once per solve
+        const double thr = tol_sq_d * df_to_double(rs_init_d);
+        thr_d.hi = (float)thr;
+        thr_d.lo = (float)(thr - (double)thr_d.hi);
+        __syncthreads();  // sh.red is reused
     } else {
-        rs_old_f = final_reduce_f32(b.part_rr, plan, sh);
+        reduce_f32(nullptr, 0u, false, rs_old_f);
         rs_init_f = rs_old_f;
     }
+
     float beta = 0.0f;
-    uint32_t k = 0;
+    uint32_t k = 0, tag = tag_base;
     for (uint32_t it = 0; it < iters; it++) {
         float* __restrict__ d_cur = (it & 1u) ? b.dB : b.dA;
         const float* __restrict__ d_prev = (it & 1u) ? b.dA : b.dB;
         const bool first = it == 0;
+        const float* __restrict__ d_src = first ? d_cur : d_prev;
         // ---------------- phase 1: direction + SpMV + d.q ----------------
         Df acc = {0.0f, 0.0f};
-        // phase-1 work on one liquid cell c with stencil mask `info`
-        auto spmv_cell = [&](size_t c, uint32_t info) -> float {
-            float dc;
-            if (first) {
-                dc = d_cur[c];
-            } else {
-                dc = __fadd_rn(r[c], __fmul_rn(beta, d_prev[c]));  // cg_dir.wgsl:30
-                d_cur[c] = dc;
-            }
-            // cg_spmv.wgsl:46-68: neighbours -x,+x,-y,+y,-z,+z
-            const size_t nbr[6] = {c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
-            float sum = 0.0f;
+        tag++;
+        {
+            uint32_t j0 = 0;
+            for (uint32_t ps = 0; ps < npc; ps++, j0 += KT) {
+                const uint32_t nb = mc - j0 < KT ? mc - j0 : KT;
+                if (multi && !f64) {
+                    for (uint32_t i = tid; i < nb * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
+                    __syncthreads();
+                }
+                const uint32_t beg = sh.pass_off[ps], end = sh.pass_off[ps + 1];
+                for (uint32_t t = beg + tid; t < end; t += 2 * CG_THREADS) {
+                    // two cells in flight: all loads first
+                    uint32_t ent[2], cc[2];
+                    float rv[2][7], dv[2][7];
 #pragma unroll
-            for (int s = 0; s < 6; s++) {
-                if (info & (2u << s)) {
-                    const float dn = first ? d_cur[nbr[s]] : __fadd_rn(r[nbr[s]], __fmul_rn(beta, d_prev[nbr[s]]));
-                    sum = __fadd_rn(sum, dn);
+                    for (int u = 0; u < 2; u++) {
+                        const uint32_t tu = t + u * CG_THREADS;
+                        const bool ok = tu < end;
+                        ent[u] = ok ? sh.cell[tu] : 0u;
+                        cc[u] = sh.chunk[ent[u] >> 18] * CHUNK + ((ent[u] >> 10) & 255u);
+                        const uint32_t c = cc[u];
+                        const uint32_t nb7[7] = {c, c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
+#pragma unroll
+                        for (int s = 0; s < 7; s++) {
+                            const bool need = ok && (s == 0 || ((ent[u] >> s) & 1u));
+                            dv[u][s] = need ? d_src[nb7[s]] : 0.0f;
+                            rv[u][s] = (need && !first) ? r[nb7[s]] : 0.0f;
+                        }
+                    }
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        if (t + u * CG_THREADS >= end) continue;
+                        const uint32_t info = ent[u];
+                        // cg_dir.wgsl:30 for the cell and its liquid neighbours,
+                        // then cg_spmv.wgsl:46-68 (order -x,+x,-y,+y,-z,+z)
+                        const float dc = first ? dv[u][0] : __fadd_rn(rv[u][0], __fmul_rn(beta, dv[u][0]));
+                        float sum = 0.0f;
+#pragma unroll
+                        for (int s = 1; s < 7; s++) {
+                            if ((info >> s) & 1u) {
+                                const float dn = first ? dv[u][s] : __fadd_rn(rv[u][s], __fmul_rn(beta, dv[u][s]));
+                                sum = __fadd_rn(sum, dn);
+                            }
+                        }
+                        const float cnt = (float)((info >> 7) & 7u);
+                        const float qc = __fsub_rn(__fmul_rn(cnt, dc), sum);
+                        const uint32_t c = cc[u];
+                        if (!first) d_cur[c] = dc;
+                        q[c] = qc;
+                        if (f64) acc = df_add(acc, df_prod(dc, qc));
+                        else sh.tree[(info >> 18) - j0][(info >> 10) & 255u] = __fmul_rn(dc, qc);
+                    }
+                }
+                if (!f64) {
+                    publish_trees(j0, nb, slotA, tag, false);
+                    if (ps + 1 < npc || mc < m) __syncthreads();
                 }
             }
-            const float cnt = (float)((info >> 7) & 7u);
-            const float qc = __fsub_rn(__fmul_rn(cnt, dc), sum);
-            q[c] = qc;
-            if (f64) acc = df_add(acc, df_prod(dc, qc));
-            return __fmul_rn(dc, qc);
-        };
-        for (uint32_t bt = 0; bt < nbt; bt++) {  // listed chunks: liquid cells only
-            const uint32_t j0 = bt * KB, nb = nkc - j0 < (uint32_t)KB ? nkc - j0 : (uint32_t)KB;
-            for (uint32_t k2 = 0; k2 < nb; k2++) sh.tree[group][k2][lt] = 0.0f;
-            named_bar(1 + group, CHUNK);
-            for (uint32_t t = sh.boff[group][bt] + lt; t < sh.boff[group][bt + 1]; t += CHUNK) {
-                const uint32_t ent = sh.cell[group][t];
-                const uint32_t j = ent >> 18, cl = (ent >> 10) & 255u;
-                const size_t c = (size_t)sh.plan[group][j] * CHUNK + cl;
-                sh.tree[group][j - j0][cl] = spmv_cell(c, ent & 1023u);
+            for (j0 = mc; j0 < m; j0 += KT) {  // chunks beyond the list: one cell slot per thread
+                const uint32_t nb = m - j0 < KT ? m - j0 : KT;
+                for (uint32_t t = tid; t < nb * CHUNK; t += CG_THREADS) {
+                    const uint32_t j = j0 + t / CHUNK, cl = t & (CHUNK - 1);
+                    const uint32_t chunk = j < KCH ? sh.chunk[j] : plan[s0 + j];
+                    const uint32_t c = chunk * CHUNK + cl;
+                    const uint32_t info = c < C ? cinfo[c] : 0u;
+                    float prod = 0.0f;
+                    if (info & 1u) {
+                        const uint32_t nb7[7] = {c, c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
+                        float dc = 0.0f, sum = 0.0f;
+#pragma unroll
+                        for (int s = 0; s < 7; s++) {
+                            if (s == 0 || ((info >> s) & 1u)) {
+                                const float dn = first ? d_src[nb7[s]]
+                                                       : __fadd_rn(r[nb7[s]], __fmul_rn(beta, d_src[nb7[s]]));
+                                if (s == 0) dc = dn;
+                                else sum = __fadd_rn(sum, dn);
+                            }
+                        }
+                        const float qc = __fsub_rn(__fmul_rn((float)((info >> 7) & 7u), dc), sum);
+                        if (!first) d_cur[c] = dc;
+                        q[c] = qc;
+                        if (f64) acc = df_add(acc, df_prod(dc, qc));
+                        prod = __fmul_rn(dc, qc);
+                    }
+                    if (!f64) sh.tree[t / CHUNK][cl] = prod;
+                }
+                if (!f64) {
+                    publish_trees(j0, nb, slotA, tag, false);
+                    __syncthreads();
+                }
             }
-            if (!f64) multi_tree(sh.tree[group], nb, group, lt, b.part_dq, gid + j0 * gstride, gstride);
-            else named_bar(1 + group, CHUNK);
         }
-        for (uint32_t j0 = nkc; j0 < nk; j0 += KB) {  // further chunks: one cell slot per thread
-            const uint32_t nb = nk - j0 < (uint32_t)KB ? nk - j0 : (uint32_t)KB;
-            for (uint32_t kb = 0; kb < nb; kb++) {
-                const uint32_t j = j0 + kb;
-                const uint32_t chunk = j < (uint32_t)KPLAN ? sh.plan[group][j] : plan[gid + j * gstride];
-                const size_t c = (size_t)chunk * CHUNK + lt;
-                const uint32_t info = c < C ? cinfo[c] : 0u;
-                sh.tree[group][kb][lt] = (info & 1u) ? spmv_cell(c, info) : 0.0f;
-            }
-            if (!f64) multi_tree(sh.tree[group], nb, group, lt, b.part_dq, gid + j0 * gstride, gstride);
-        }
-        if (f64) {
-            __syncthreads();
-            block_sum_df(acc, &cta64[blockIdx.x], sh);
-        }
-        target += G;
-        if (!grid_barrier(b.st, target, sh)) return;
         float alpha;
         if (f64) {
-            const double dq = final_reduce_f64(cta64, G, sh);
-            alpha = fabs(dq) > 1e-30 ? (float)(rs_old_d / dq) : 0.0f;
+            publish_df(acc, wordA, tag, false);
+            Df dq;
+            if (!reduce_df(wordA, tag, false, dq)) return;
+            alpha = fabsf(dq.hi) > 1e-30f ? df_div(rs_old_d, dq) : 0.0f;
         } else {
-            const float dq = final_reduce_f32(b.part_dq, nullptr, sh);
+            float dq;
+            if (!reduce_f32(slotA, tag, false, dq)) return;
             alpha = fabsf(dq) > 1e-30f ? __fdiv_rn(rs_old_f, dq) : 0.0f;  // cg_alpha.wgsl:17-22
         }
         // ---------------- phase 2: update + r.r ----------------
         acc = {0.0f, 0.0f};
-        auto update_cell = [&](size_t c) -> float {
-            p[c] = __fadd_rn(p[c], __fmul_rn(alpha, d_cur[c]));      // cg_update.wgsl:33
-            const float rc = __fsub_rn(r[c], __fmul_rn(alpha, q[c]));  // cg_update.wgsl:34
-            r[c] = rc;
-            if (f64) acc = df_add(acc, df_prod(rc, rc));
-            return __fmul_rn(rc, rc);
-        };
-        for (uint32_t bt = 0; bt < nbt; bt++) {
-            const uint32_t j0 = bt * KB, nb = nkc - j0 < (uint32_t)KB ? nkc - j0 : (uint32_t)KB;
-            for (uint32_t k2 = 0; k2 < nb; k2++) sh.tree[group][k2][lt] = 0.0f;
-            named_bar(1 + group, CHUNK);
-            for (uint32_t t = sh.boff[group][bt] + lt; t < sh.boff[group][bt + 1]; t += CHUNK) {
-                const uint32_t ent = sh.cell[group][t];
-                const uint32_t j = ent >> 18, cl = (ent >> 10) & 255u;
-                const size_t c = (size_t)sh.plan[group][j] * CHUNK + cl;
-                sh.tree[group][j - j0][cl] = update_cell(c);
+        tag++;
+        {
+            uint32_t j0 = 0;
+            for (uint32_t ps = 0; ps < npc; ps++, j0 += KT) {
+                const uint32_t nb = mc - j0 < KT ? mc - j0 : KT;
+                if (multi && !f64) {
+                    for (uint32_t i = tid; i < nb * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
+                    __syncthreads();
+                }
+                const uint32_t beg = sh.pass_off[ps], end = sh.pass_off[ps + 1];
+                for (uint32_t t = beg + tid; t < end; t += 2 * CG_THREADS) {
+                    uint32_t ent[2], cc[2];
+                    float pv[2], dv[2], rv[2], qv[2];
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        const uint32_t tu = t + u * CG_THREADS;
+                        const bool ok = tu < end;
+                        ent[u] = ok ? sh.cell[tu] : 0u;
+                        cc[u] = sh.chunk[ent[u] >> 18] * CHUNK + ((ent[u] >> 10) & 255u);
+                        pv[u] = ok ? p[cc[u]] : 0.0f;
+                        dv[u] = ok ? d_cur[cc[u]] : 0.0f;
+                        rv[u] = ok ? r[cc[u]] : 0.0f;
+                        qv[u] = ok ? q[cc[u]] : 0.0f;
+                    }
+#pragma unroll
+                    for (int u = 0; u < 2; u++) {
+                        if (t + u * CG_THREADS >= end) continue;
+                        const uint32_t c = cc[u];
+                        p[c] = __fadd_rn(pv[u], __fmul_rn(alpha, dv[u]));       // cg_update.wgsl:33
+                        const float rc = __fsub_rn(rv[u], __fmul_rn(alpha, qv[u]));  // cg_update.wgsl:34
+                        r[c] = rc;
+                        if (f64) acc = df_add(acc, df_prod(rc, rc));
+                        else sh.tree[(ent[u] >> 18) - j0][(ent[u] >> 10) & 255u] = __fmul_rn(rc, rc);
+                    }
+                }
+                if (!f64) {
+                    publish_trees(j0, nb, slotB, tag, true);
+                    if (ps + 1 < npc || mc < m) __syncthreads();
+                }
             }
-            if (!f64) multi_tree(sh.tree[group], nb, group, lt, b.part_rr, gid + j0 * gstride, gstride);
-            else named_bar(1 + group, CHUNK);
-        }
-        for (uint32_t j0 = nkc; j0 < nk; j0 += KB) {
-            const uint32_t nb = nk - j0 < (uint32_t)KB ? nk - j0 : (uint32_t)KB;
-            for (uint32_t kb = 0; kb < nb; kb++) {
-                const uint32_t j = j0 + kb;
-                const uint32_t chunk = j < (uint32_t)KPLAN ? sh.plan[group][j] : plan[gid + j * gstride];
-                const size_t c = (size_t)chunk * CHUNK + lt;
-                const uint32_t info = c < C ? cinfo[c] : 0u;
-                sh.tree[group][kb][lt] = (info & 1u) ? update_cell(c) : 0.0f;
+            for (j0 = mc; j0 < m; j0 += KT) {
+                const uint32_t nb = m - j0 < KT ? m - j0 : KT;
+                for (uint32_t t = tid; t < nb * CHUNK; t += CG_THREADS) {
+                    const uint32_t j = j0 + t / CHUNK, cl = t & (CHUNK - 1);
+                    const uint32_t chunk = j < KCH ? sh.chunk[j] : plan[s0 + j];
+                    const uint32_t c = chunk * CHUNK + cl;
+                    const uint32_t info = c < C ? cinfo[c] : 0u;
+                    float prod = 0.0f;
+                    if (info & 1u) {
+                        p[c] = __fadd_rn(p[c], __fmul_rn(alpha, d_cur[c]));
+                        const float rc = __fsub_rn(r[c], __fmul_rn(alpha, q[c]));
+                        r[c] = rc;
+                        if (f64) acc = df_add(acc, df_prod(rc, rc));
+                        prod = __fmul_rn(rc, rc);
+                    }
+                    if (!f64) sh.tree[t / CHUNK][cl] = prod;
+                }
+                if (!f64) {
+                    publish_trees(j0, nb, slotB, tag, true);
+                    __syncthreads();
+                }
             }
-            if (!f64) multi_tree(sh.tree[group], nb, group, lt, b.part_rr, gid + j0 * gstride, gstride);
         }
-        if (f64) {
-            __syncthreads();
-            block_sum_df(acc, &cta64[G + blockIdx.x], sh);
-        }
-        target += G;
-        if (!grid_barrier(b.st, target, sh)) return;
         k = it + 1;
         bool done;
         if (f64) {
-            const double rs_new = final_reduce_f64(cta64 + G, G, sh);
-            beta = rs_old_d > 1e-30 ? (float)(rs_new / rs_old_d) : 0.0f;
+            publish_df(acc, wordB, tag, true);
+            Df rs_new;
+            if (!reduce_df(wordB, tag, true, rs_new)) return;
+            beta = rs_old_d.hi > 1e-30f ? df_div(rs_new, rs_old_d) : 0.0f;
             rs_old_d = rs_new;
-            done = P.tol_sq_d > 0.0 && rs_new <= P.tol_sq_d * rs_init_d;
+            done = tol_sq_d > 0.0 && df_le(rs_new, thr_d);
         } else {
-            const float rs_new = final_reduce_f32(b.part_rr, nullptr, sh);
+            float rs_new;
+            if (!reduce_f32(slotB, tag, true, rs_new)) return;
             beta = rs_old_f > 1e-30f ? __fdiv_rn(rs_new, rs_old_f) : 0.0f;  // cg_beta.wgsl:16-23
             rs_old_f = rs_new;
-            done = P.tol_sq > 0.0f && rs_new <= __fmul_rn(P.tol_sq, rs_init_f);  // cg_beta.wgsl:25-30
+            done = tol_sq > 0.0f && rs_new <= __fmul_rn(tol_sq, rs_init_f);  // cg_beta.wgsl:25-30
         }
         if (done) break;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        b.st->cg_iters = k;
-        b.st->rs_init = f64 ? rs_init_d : (double)rs_init_f;
-        b.st->rs_final = f64 ? rs_old_d : (double)rs_old_f;
+    if (blockIdx.x == 0 && tid == 0) {
+        st->cg_iters = k;
+        st->rs_init = f64 ? df_to_double(rs_init_d) : (double)rs_init_f;
+        st->rs_final = f64 ? df_to_double(rs_old_d) : (double)rs_old_f;
     }
 }
 
 int cg_max_blocks_per_sm() {
-    if (cudaFuncSetAttribute(k_cg, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CgShared)) != cudaSuccess)
-        return 0;
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_cg, CG_THREADS, sizeof(CgShared)) != cudaSuccess) return 0;
-    return n;
+    int n[2] = {0, 0};
+    for (int i = 0; i < 2; i++) {
+        const void* f = i ? (const void*)k_cg<true> : (const void*)k_cg<false>;
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CgShared)) != cudaSuccess)
+            return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n[i], f, CG_THREADS, sizeof(CgShared)) != cudaSuccess) return 0;
+    }
+    return n[0] < n[1] ? n[0] : n[1];
 }
 
-cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s) {
-    k_cg_plan<<<1, CHUNK, 0, s>>>(b);
+cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, bool f64) {
+    if (L.cg_blocks < 1 || (uint32_t)L.cg_blocks > MAX_CG_BLOCKS) return cudaErrorInvalidValue;
+    k_cg_plan<<<1, CHUNK, 0, s>>>(b, (uint32_t)L.cg_blocks);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
@@ -454,7 +710,7 @@ cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_cg, b);
+    return f64 ? cudaLaunchKernelEx(&cfg, k_cg<true>, b) : cudaLaunchKernelEx(&cfg, k_cg<false>, b);
 }
 
 }  // namespace fl

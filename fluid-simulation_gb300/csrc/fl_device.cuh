@@ -76,19 +76,31 @@ struct DevBufs {
     uint8_t* ct;
     uint16_t* cinfo;       // per liquid cell: bit0 liquid, bits1-6 liquid neighbours (-x,+x,-y,+y,-z,+z),
                            // bits 7-9 count of non-solid neighbours (cg_spmv.wgsl:46-66); 0 elsewhere
-    uint8_t* chunk_flag;
+    uint8_t* chunk_flag;   // liquid cells of each 256-cell chunk, saturated at 255 (0: none)
     int32_t* num[3];
     int32_t* den[3];
     float* vel[3];
     float* sav[3];
     float *p, *r, *dA, *dB, *q;
-    float* part_rr;        // per-chunk f32 tree partials
-    float* part_dq;
-    double* chunk_rr64;    // per-chunk f64 partials of the initial residual
-    double* cta_part64;    // [2][max CTAs] f64 partials (FL_CG_F64)
+    float* part_rr;        // per-chunk f32 tree partials of the initial residual
+    float2* chunk_rr_df;   // per-chunk float-float partials {hi, lo} of the initial residual
     uint32_t* cg_chunk;    // CG plan: active chunks grouped by (chunk mod 256), ascending
-    uint32_t* cg_off;      // CG plan: 257 segment offsets into cg_chunk
+    uint32_t* cg_off;      // CG plan header, cg_plan_words(max blocks) words: 257 segment
+                           // offsets into cg_chunk, the launch's tag base, the slot
+                           // line stride, then the first plan entry of every block
+                           // (blocks + 1 entries)
+    unsigned long long* cg_x;  // CG exchange words, cg_x_words(nchunks, max blocks): [0] tag
+                               // epoch (persists across solves), then tagged partials
 };
+
+// Sizes of the CG plan header and exchange area (fl_cg.cu).
+#if defined(__CUDACC__)
+#define FL_HD __host__ __device__
+#else
+#define FL_HD
+#endif
+FL_HD constexpr size_t cg_plan_words(size_t max_blocks) { return (size_t)CHUNK + 3 + max_blocks + 1; }
+FL_HD constexpr size_t cg_x_words(size_t nchunks, size_t max_blocks) { return 8 + 2 * nchunks + 64 * max_blocks; }
 
 // Buffers of one adjoint step (fl_adjoint.cu).
 struct AdjBufs {
@@ -118,6 +130,49 @@ struct AdjBufs {
 // ---------------------------------------------------------------------------
 // helpers (device code only; fl_host.cpp sees the layout above)
 #if defined(__CUDACC__)
+
+// Float-float ("double-single") arithmetic: a value is hi + lo with two f32,
+// |lo| <= ulp(hi)/2, about 48 significand bits.  GB300's FP64 pipe has a
+// dependent-op latency of ~64 cycles for one warp and ~600 with a full SM
+// issuing (DDIV ~640 for one warp), so the FL_CG_F64 inner products, residual
+// norms and stopping test are carried in float-float on the FP32 pipe
+// (df_add: ~32 cycles dependent latency) and converted to double only for the
+// statistics.  Products use the exact two-product (fmaf), sums the two-sum.
+struct Df {
+    float hi, lo;
+};
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+    const float s = __fadd_rn(a.hi, b.hi);
+    const float bb = __fsub_rn(s, a.hi);
+    float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, bb)), __fsub_rn(b.hi, bb));
+    e = __fadd_rn(e, __fadd_rn(a.lo, b.lo));
+    const float hi = __fadd_rn(s, e);
+    return {hi, __fsub_rn(e, __fsub_rn(hi, s))};
+}
+__device__ __forceinline__ Df df_prod(float x, float y) {
+    const float p = __fmul_rn(x, y);
+    return {p, __fmaf_rn(x, y, -p)};
+}
+__device__ __forceinline__ Df warp_sum_df(Df v) {  // result in lane 0
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Df w;
+        w.hi = __shfl_down_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_down_sync(0xffffffffu, v.lo, o);
+        v = df_add(v, w);
+    }
+    return v;
+}
+__device__ __forceinline__ Df warp_allsum_df(Df v) {  // result in every lane
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        Df w;
+        w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+        w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+        v = df_add(v, w);
+    }
+    return v;
+}
 
 __device__ __forceinline__ uint32_t face_dim(const DevParams& P, int axis, int b) {
     uint32_t n = b == 0 ? P.nx : (b == 1 ? P.ny : P.nz);
@@ -193,7 +248,8 @@ cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s);
 cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz,
                        cudaStream_t s);
 cudaError_t launch_grid_prep(const DevBufs& b, uint32_t C, cudaStream_t s);
-cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
+// f64: FL_CG_F64 (the kernel is specialised per precision).
+cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, bool f64);
 cudaError_t launch_project(const DevBufs& b, uint32_t C, cudaStream_t s);
 cudaError_t launch_g2p(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_iota(uint32_t* ids, uint32_t n, cudaStream_t s);

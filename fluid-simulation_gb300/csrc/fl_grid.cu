@@ -294,13 +294,13 @@ __device__ __forceinline__ uint16_t stencil_info(const uint8_t* ct, size_t c, si
 
 __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
     __shared__ float s_tree[256];
-    __shared__ double s_red[8];
+    __shared__ float2 s_red[8];
     const DevParams& P = *b.prm;
     const uint32_t chunk = blockIdx.x;
     const uint32_t c = chunk * 256 + threadIdx.x;
     bool liquid = false;
     float prod = 0.0f;
-    double prod64 = 0.0;
+    Df pdf = {0.0f, 0.0f};
     if (c < C) {
         const uint32_t nx = P.nx, ny = P.ny, nz = P.nz;
         const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
             b.dA[c] = rc;
             b.cinfo[c] = stencil_info(b.ct, c, nx, (size_t)nx * ny);
             prod = __fmul_rn(rc, rc);
-            prod64 = (double)rc * (double)rc;
+            pdf = df_prod(rc, rc);
         } else {
             b.p[c] = 0.0f;
             b.r[c] = 0.0f;
@@ -346,20 +346,18 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
             b.cinfo[c] = 0;
         }
     }
-    const int any = __syncthreads_or(liquid);
+    const int nliq = __syncthreads_count(liquid);
     const float v = block_tree256(prod, s_tree);
-    // f64 partial of this chunk (fixed order: warp shuffles, then warps in order)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) prod64 += __shfl_down_sync(0xffffffffu, prod64, o);
-    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = prod64;
+    // float-float partial of this chunk (fixed order: warp shuffles, then warps in order)
+    pdf = warp_sum_df(pdf);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = make_float2(pdf.hi, pdf.lo);
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0;
-        for (int w = 0; w < 8; w++) a += s_red[w];
+        Df a = {0.0f, 0.0f};
+        for (int w = 0; w < 8; w++) a = df_add(a, Df{s_red[w].x, s_red[w].y});
         b.part_rr[chunk] = v;
-        b.part_dq[chunk] = 0.0f;
-        b.chunk_rr64[chunk] = a;
-        b.chunk_flag[chunk] = any ? 1 : 0;
+        b.chunk_rr_df[chunk] = make_float2(a.hi, a.lo);
+        b.chunk_flag[chunk] = (uint8_t)(nliq < 255 ? nliq : 255);
     }
 }
 
@@ -394,13 +392,13 @@ __global__ void __launch_bounds__(256) k_project(DevBufs b, uint32_t C) {
 // tail of k_grid_prep without the face passes).
 __global__ void __launch_bounds__(256) k_solve_init(DevBufs b, uint32_t C, const float* __restrict__ div) {
     __shared__ float s_tree[256];
-    __shared__ double s_red[8];
+    __shared__ float2 s_red[8];
     const DevParams& P = *b.prm;
     const uint32_t chunk = blockIdx.x;
     const uint32_t c = chunk * 256 + threadIdx.x;
     bool liquid = false;
     float prod = 0.0f;
-    double prod64 = 0.0;
+    Df pdf = {0.0f, 0.0f};
     if (c < C) {
         liquid = b.ct[c] == CELL_LIQUID;
         if (liquid) {
@@ -417,7 +415,7 @@ __global__ void __launch_bounds__(256) k_solve_init(DevBufs b, uint32_t C, const
             b.dA[c] = rc;
             b.cinfo[c] = stencil_info(b.ct, c, P.nx, (size_t)P.nx * P.ny);
             prod = __fmul_rn(rc, rc);
-            prod64 = (double)rc * (double)rc;
+            pdf = df_prod(rc, rc);
         } else {
             b.p[c] = 0.0f;
             b.r[c] = 0.0f;
@@ -425,19 +423,18 @@ __global__ void __launch_bounds__(256) k_solve_init(DevBufs b, uint32_t C, const
             b.cinfo[c] = 0;
         }
     }
-    const int any = __syncthreads_or(liquid);
+    const int nliq = __syncthreads_count(liquid);
     const float v = block_tree256(prod, s_tree);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) prod64 += __shfl_down_sync(0xffffffffu, prod64, o);
-    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = prod64;
+    // float-float partial of this chunk (fixed order: warp shuffles, then warps in order)
+    pdf = warp_sum_df(pdf);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = make_float2(pdf.hi, pdf.lo);
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0;
-        for (int w = 0; w < 8; w++) a += s_red[w];
+        Df a = {0.0f, 0.0f};
+        for (int w = 0; w < 8; w++) a = df_add(a, Df{s_red[w].x, s_red[w].y});
         b.part_rr[chunk] = v;
-        b.part_dq[chunk] = 0.0f;
-        b.chunk_rr64[chunk] = a;
-        b.chunk_flag[chunk] = any ? 1 : 0;
+        b.chunk_rr_df[chunk] = make_float2(a.hi, a.lo);
+        b.chunk_flag[chunk] = (uint8_t)(nliq < 255 ? nliq : 255);
     }
 }
 

@@ -189,7 +189,7 @@ cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEve
     if ((e = mark(3)) != cudaSuccess) return e;
     if ((e = fl::launch_grid_prep(b, h->C, s)) != cudaSuccess) return e;
     if ((e = mark(4)) != cudaSuccess) return e;
-    if ((e = fl::launch_cg(b, h->L, s)) != cudaSuccess) return e;
+    if ((e = fl::launch_cg(b, h->L, s, h->prm.cg_precision == FL_CG_F64)) != cudaSuccess) return e;
     if ((e = mark(5)) != cudaSuccess) return e;
     if ((e = fl::launch_project(b, h->C, s)) != cudaSuccess) return e;
     if ((e = mark(6)) != cudaSuccess) return e;
@@ -335,10 +335,10 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     }
     size_t o_p = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C), o_dB = pl.take<float>(C),
            o_q = pl.take<float>(C);
-    size_t o_prr = pl.take<float>(h->nchunks), o_pdq = pl.take<float>(h->nchunks);
-    size_t o_c64 = pl.take<double>(h->nchunks);
-    size_t o_cta = pl.take<double>(2 * (size_t)g_num_sms * g_cg_per_sm);
-    size_t o_plan = pl.take<uint32_t>(h->nchunks), o_poff = pl.take<uint32_t>(fl::CHUNK + 1);
+    const size_t gmax = (size_t)g_num_sms * g_cg_per_sm;
+    size_t o_prr = pl.take<float>(h->nchunks), o_c64 = pl.take<float2>(h->nchunks);
+    size_t o_plan = pl.take<uint32_t>(h->nchunks), o_poff = pl.take<uint32_t>(fl::cg_plan_words(gmax));
+    size_t o_cgx = pl.take<unsigned long long>(fl::cg_x_words(h->nchunks, gmax));
     size_t o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
     h->pool_bytes = pl.off;
 
@@ -395,11 +395,10 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     b.dB = (float*)(base + o_dB);
     b.q = (float*)(base + o_q);
     b.part_rr = (float*)(base + o_prr);
-    b.part_dq = (float*)(base + o_pdq);
-    b.chunk_rr64 = (double*)(base + o_c64);
-    b.cta_part64 = (double*)(base + o_cta);
+    b.chunk_rr_df = (float2*)(base + o_c64);
     b.cg_chunk = (uint32_t*)(base + o_plan);
     b.cg_off = (uint32_t*)(base + o_poff);
+    b.cg_x = (unsigned long long*)(base + o_cgx);
     if ((s = upload_params(h)) != FL_OK) {
         std::string m = h->err;
         fl_destroy(h);
@@ -427,6 +426,12 @@ fl_status fl_set_params(fl_handle* h, const fl_params* params) {
     if (validate(params, &why) != FL_OK) return set_err(h, FL_INVALID_ARG, why);
     if (params->gdim[0] != h->nx || params->gdim[1] != h->ny || params->gdim[2] != h->nz)
         return set_err(h, FL_INVALID_ARG, "grid dimensions cannot change on a live handle; create a new one");
+    if (params->cg_precision != h->prm.cg_precision && h->graph) {
+        // the CG kernel is specialised per precision: capture the step again
+        FL_CUDA(h, cudaStreamSynchronize(h->stream));
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
     h->prm = *params;
     return upload_params(h);
 }
@@ -774,10 +779,11 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     PoolPlan pl;
     size_t o_ct = pl.take<uint8_t>(C), o_div = pl.take<float>(C), o_p = pl.take<float>(C), o_r = pl.take<float>(C),
            o_dA = pl.take<float>(C), o_dB = pl.take<float>(C), o_q = pl.take<float>(C);
-    size_t o_flag = pl.take<uint8_t>(nchunks), o_prr = pl.take<float>(nchunks), o_pdq = pl.take<float>(nchunks);
+    size_t o_flag = pl.take<uint8_t>(nchunks), o_prr = pl.take<float>(nchunks);
     size_t o_cinfo = pl.take<uint16_t>(C);
-    size_t o_c64 = pl.take<double>(nchunks), o_cta = pl.take<double>(2 * (size_t)L.cg_blocks);
-    size_t o_plan = pl.take<uint32_t>(nchunks), o_poff = pl.take<uint32_t>(fl::CHUNK + 1);
+    size_t o_c64 = pl.take<float2>(nchunks);
+    size_t o_plan = pl.take<uint32_t>(nchunks), o_poff = pl.take<uint32_t>(fl::cg_plan_words(L.cg_blocks));
+    size_t o_cgx = pl.take<unsigned long long>(fl::cg_x_words(nchunks, L.cg_blocks));
     size_t o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
     void* pool = nullptr;
     cudaError_t e = cudaMalloc(&pool, pl.off);
@@ -798,11 +804,10 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     b.chunk_flag = (uint8_t*)(base + o_flag);
     b.cinfo = (uint16_t*)(base + o_cinfo);
     b.part_rr = (float*)(base + o_prr);
-    b.part_dq = (float*)(base + o_pdq);
-    b.chunk_rr64 = (double*)(base + o_c64);
-    b.cta_part64 = (double*)(base + o_cta);
+    b.chunk_rr_df = (float2*)(base + o_c64);
     b.cg_chunk = (uint32_t*)(base + o_plan);
     b.cg_off = (uint32_t*)(base + o_poff);
+    b.cg_x = (unsigned long long*)(base + o_cgx);
     float* ddiv = (float*)(base + o_div);
     cudaStream_t st = nullptr;
     fl_status rs = FL_OK;
@@ -815,7 +820,7 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
         if ((e = cudaMemcpyAsync(ddiv, divergence, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
         if (warm_start && (e = cudaMemcpyAsync(b.p, pressure_in, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
         if ((e = fl::launch_solve_init(b, (uint32_t)C, ddiv, st)) != cudaSuccess) break;
-        if ((e = fl::launch_cg(b, L, st)) != cudaSuccess) break;
+        if ((e = fl::launch_cg(b, L, st, cg_precision == FL_CG_F64)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(pressure_out, b.p, 4 * C, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(&ds, b.st, sizeof(ds), cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
         e = cudaStreamSynchronize(st);
@@ -890,6 +895,7 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     t->h = h;
     t->max_steps = max_steps;
     const size_t cap = std::max<uint32_t>(h->cap, 1), C = h->C, nch = h->nchunks;
+    const size_t gmax = (size_t)g_num_sms * g_cg_per_sm;
     PoolPlan slot;
     t->o_part = slot.take<float4>(2 * cap);
     t->o_perm = slot.take<uint32_t>(cap);
@@ -909,10 +915,11 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     }
     size_t o_rhs = pl.take<float>(C), o_lam = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C),
            o_dB = pl.take<float>(C), o_q = pl.take<float>(C), o_ci = pl.take<uint16_t>(C), o_fl = pl.take<uint8_t>(nch),
-           o_prr = pl.take<float>(nch), o_pdq = pl.take<float>(nch), o_c64 = pl.take<double>(nch),
-           o_cta = pl.take<double>(2 * (size_t)g_num_sms * g_cg_per_sm), o_plan = pl.take<uint32_t>(nch),
-           o_poff = pl.take<uint32_t>(fl::CHUNK + 1), o_gg = pl.take<double>(3), o_prm = pl.take<DevParams>(1),
-           o_st = pl.take<DevStats>(1);
+           o_prr = pl.take<float>(nch), o_c64 = pl.take<float2>(nch), o_plan = pl.take<uint32_t>(nch),
+           o_poff = pl.take<uint32_t>(fl::cg_plan_words(gmax)), o_gg = pl.take<double>(3),
+           o_prm = pl.take<DevParams>(1), o_st = pl.take<DevStats>(1);
+    const size_t cgx_words = fl::cg_x_words(nch, gmax);
+    const size_t o_cgx = pl.take<unsigned long long>(cgx_words);
     cudaError_t e = cudaMalloc(&t->pool, pl.off);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
@@ -940,11 +947,18 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     b.cinfo = (uint16_t*)(base + o_ci);
     b.chunk_flag = (uint8_t*)(base + o_fl);
     b.part_rr = (float*)(base + o_prr);
-    b.part_dq = (float*)(base + o_pdq);
-    b.chunk_rr64 = (double*)(base + o_c64);
-    b.cta_part64 = (double*)(base + o_cta);
+    b.chunk_rr_df = (float2*)(base + o_c64);
     b.cg_chunk = (uint32_t*)(base + o_plan);
     b.cg_off = (uint32_t*)(base + o_poff);
+    b.cg_x = (unsigned long long*)(base + o_cgx);
+    // The exchange words start cleared (tags of an earlier owner of this
+    // memory must not match).
+    if ((e = cudaMemsetAsync(b.cg_x, 0, cgx_words * sizeof(unsigned long long), h->stream)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) {
+        cudaFree(t->pool);
+        delete t;
+        return cuda_err(h, e, "tape exchange-area clear");
+    }
     *out = t;
     return FL_OK;
 }
@@ -1050,7 +1064,7 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     FL_CUDA(h, cudaMemcpyAsync((void*)cg.prm, &t->hp_cg, sizeof(DevParams), cudaMemcpyHostToDevice, st));
     FL_CUDA(h, cudaMemsetAsync(cg.st, 0, sizeof(DevStats), st));
     FL_CUDA(h, fl::launch_solve_init(cg, h->C, t->rhs, st));
-    FL_CUDA(h, fl::launch_cg(cg, h->L, st));
+    FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
     FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));
     for (int ax = 0; ax < 3; ax++) {
         FL_CUDA(h, cudaMemsetAsync(a.w_sum[ax], 0, 4 * (size_t)h->F3[ax], st));

@@ -10,12 +10,14 @@
 // output as device pointers; this entry point allocates nothing.
 //
 // The scratch (CG vectors r, d (two copies), q, the stencil masks, per-chunk
-// partials, the solve plan, the settings block and the device counters) lives in `g_noalloc_scratch`, sized
-// for at most FL_NOALLOC_MAX_CELLS cells (~4.6 MB).  Every GPU that loads this
-// library holds that array until the process exits.  All calls share it: a
-// call keeps the previous call's contents, so the set-up kernel clears what
-// must start at zero (the barrier counter and the status word), and calls that
-// overlap on the GPU (different streams, or different host threads) race on it.
+// partials, the solve plan, the exchange words, the settings block and the
+// device counters) lives in `g_noalloc_scratch`, sized for at most
+// FL_NOALLOC_MAX_CELLS cells (~4.6 MB).  Every GPU that loads this library
+// holds that array until the process exits.  All calls share it: a call keeps
+// the previous call's contents, so the set-up kernel clears what must start at
+// zero (the counters and the status word; the exchange words carry tags that
+// are unique per solve and need no clearing), and calls that overlap on the
+// GPU (different streams, or different host threads) race on it.
 //
 // In host code `g_noalloc_scratch` is a host-side stand-in, not a device
 // address.  The device address is obtained once per device, with that device
@@ -33,7 +35,7 @@
 
 namespace {
 
-constexpr size_t kMaxCtas = 1024;  // per-slot capacity of the f64 block partials
+constexpr size_t kMaxCtas = 1024;  // cooperative blocks the plan header and exchange area are sized for
 constexpr size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 // Scratch layout (byte offsets), sized for FL_NOALLOC_MAX_CELLS cells.
@@ -47,13 +49,12 @@ constexpr size_t kOffDB = align256(kOffDA + 4 * kCells);
 constexpr size_t kOffQ = align256(kOffDB + 4 * kCells);
 constexpr size_t kOffFlag = align256(kOffQ + 4 * kCells);
 constexpr size_t kOffPrr = align256(kOffFlag + kChunks);
-constexpr size_t kOffPdq = align256(kOffPrr + 4 * kChunks);
-constexpr size_t kOffC64 = align256(kOffPdq + 4 * kChunks);
-constexpr size_t kOffCta = align256(kOffC64 + 8 * kChunks);
-constexpr size_t kOffPlan = align256(kOffCta + 8 * 2 * kMaxCtas);
+constexpr size_t kOffC64 = align256(kOffPrr + 4 * kChunks);
+constexpr size_t kOffPlan = align256(kOffC64 + 8 * kChunks);
 constexpr size_t kOffPlanOff = align256(kOffPlan + 4 * kChunks);
-constexpr size_t kOffInfo = align256(kOffPlanOff + 4 * (fl::CHUNK + 1));
-constexpr size_t kScratchBytes = align256(kOffInfo + 2 * kCells);
+constexpr size_t kOffInfo = align256(kOffPlanOff + 4 * fl::cg_plan_words(kMaxCtas));
+constexpr size_t kOffX = align256(kOffInfo + 2 * kCells);
+constexpr size_t kScratchBytes = align256(kOffX + 8 * fl::cg_x_words(kChunks, kMaxCtas));
 
 constexpr int kMaxDevices = 64;
 
@@ -165,19 +166,18 @@ extern "C" fl_status fl_solve_pressure_noalloc(uint32_t nx, uint32_t ny, uint32_
     b.q = (float*)(base + kOffQ);
     b.chunk_flag = (uint8_t*)(base + kOffFlag);
     b.part_rr = (float*)(base + kOffPrr);
-    b.part_dq = (float*)(base + kOffPdq);
-    b.chunk_rr64 = (double*)(base + kOffC64);
-    b.cta_part64 = (double*)(base + kOffCta);
+    b.chunk_rr_df = (float2*)(base + kOffC64);
     b.cg_chunk = (uint32_t*)(base + kOffPlan);
     b.cg_off = (uint32_t*)(base + kOffPlanOff);
     b.cinfo = (uint16_t*)(base + kOffInfo);
+    b.cg_x = (unsigned long long*)(base + kOffX);
 
     cudaStream_t st = (cudaStream_t)cuda_stream;
     k_noalloc_setup<<<1, 32, 0, st>>>(d, (fl::DevParams*)(base + kOffParams), b.st);
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(FL_CUDA_ERROR, std::string("setup: ") + cudaGetErrorString(e));
     if ((e = fl::launch_solve_init(b, d.C, divergence_dev, st)) != cudaSuccess)
         return fail(FL_CUDA_ERROR, std::string("init: ") + cudaGetErrorString(e));
-    if ((e = fl::launch_cg(b, L, st)) != cudaSuccess)
+    if ((e = fl::launch_cg(b, L, st, cg_precision == FL_CG_F64)) != cudaSuccess)
         return fail(FL_CUDA_ERROR, std::string("cg: ") + cudaGetErrorString(e));
     fl::DevStats ds;
     if ((e = cudaMemcpyAsync(&ds, b.st, sizeof(ds), cudaMemcpyDeviceToHost, st)) != cudaSuccess)

@@ -41,14 +41,20 @@
 namespace fl {
 
 constexpr int CG_WARPS = CG_THREADS / 32;
-constexpr uint32_t KT = CG_WARPS;        // chunks per tree pass: one chunk tree per warp
+constexpr uint32_t KT = 2 * CG_WARPS;    // chunks per tree pass: two chunk trees per warp
 constexpr uint32_t CELL_CAP = 16384;     // liquid cells listed per block
 constexpr uint32_t KCH = 2048;           // chunk ids cached per block
-constexpr uint32_t VAL_CAP = 20480;      // chunk partials staged per window
+constexpr uint32_t VAL_CAP = 16384;      // chunk partials staged per window
 constexpr uint32_t MAX_PASS = KCH / KT;  // cached tree passes
 constexpr uint32_t TAG_SPAN_MAX = 1u << 30;
-constexpr int STAGE_BATCH = 4;
+constexpr int STAGE_BATCH = 8;
 constexpr uint32_t MAX_CG_BLOCKS = 1024;
+// Per-chunk cost in liquid-cell units for the block split (each chunk adds a
+// tree and, when sparsely filled, cells that share few cache lines).  Kept
+// small: a block above 2 * CG_THREADS listed cells needs a second, serial
+// round of the cell loop, which costs more than the chunk overhead (measured
+// on the 128^3 dam break; 128 pushed dense blocks past that threshold).
+constexpr uint32_t CHUNK_WEIGHT = 32;
 
 struct CgShared {
     float tree[KT][CHUNK];     // per-chunk products of one pass, tree slot = cell in chunk
@@ -62,6 +68,7 @@ struct CgShared {
     uint32_t wcnt[CG_WARPS];
     uint32_t bstart[MAX_CG_BLOCKS + 1];  // first plan entry of every block
 };
+static_assert(sizeof(CgShared) <= 227 * 1024, "CG shared memory exceeds the 227 KB per-block limit");
 
 // ---------------------------------------------------------------------------
 // Tagged words
@@ -89,6 +96,9 @@ __device__ __forceinline__ void publish(unsigned long long* p, uint32_t tag, flo
     if (rel) st_release_u64(p, w);
     else st_relaxed_u64(p, w);
 }
+// Polls of an exchange after which the reader loads other blocks' vector
+// writes are acquire loads (measured faster than relaxed polls followed by an
+// acquire fence in every thread); the other exchange polls relaxed.
 __device__ __forceinline__ unsigned long long ld_tag(const unsigned long long* p, bool acq) {
     return acq ? ld_acquire_u64(p) : ld_relaxed_u64(p);
 }
@@ -113,31 +123,34 @@ __device__ __noinline__ unsigned long long wait_tag(const unsigned long long* p,
     return w;
 }
 
-// Stages words x[e0 + i*stride(i)] for i < n (all carrying `tag`) into vals[i]:
-// STAGE_BATCH loads in flight per thread.  Word i sits at (i / per) * 16 + i % per
-// when per != 0 (`per` words of each block on their own 128-byte line), else
-// at e0 + i.  Returns false on abort.
-__device__ __forceinline__ bool stage_tagged(const unsigned long long* x, uint32_t e0, uint32_t n, uint32_t tag,
-                                             float* vals, DevStats* st, bool acq, uint32_t per = 0) {
+// Stages tagged words: for each virtual index v < nvirt, addr(v) is the word
+// (nullptr: unused index) and dst(v) its slot in vals.  A thread issues up to
+// STAGE_BATCH loads at once, then waits for its unpublished words one at a
+// time (one poll in flight per thread keeps the traffic on the shared lines
+// low; measured faster than re-polling all pending words together).
+// Returns false on abort.
+template <class AddrF, class DstF>
+__device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool acq, DevStats* st, float* vals,
+                                            AddrF addr, DstF dst) {
     bool ok = true;
-    for (uint32_t i0 = threadIdx.x; i0 < n; i0 += STAGE_BATCH * CG_THREADS) {
+    for (uint32_t v0 = threadIdx.x; v0 < nvirt; v0 += STAGE_BATCH * CG_THREADS) {
         unsigned long long w[STAGE_BATCH];
 #pragma unroll
         for (int k = 0; k < STAGE_BATCH; k++) {
-            const uint32_t i = i0 + k * CG_THREADS;
-            const uint32_t at = per ? (i / per) * 16u + i % per : e0 + i;
-            w[k] = i < n ? ld_tag(x + at, acq) : 0ull;
+            const uint32_t v = v0 + k * CG_THREADS;
+            const unsigned long long* a = v < nvirt ? addr(v) : nullptr;
+            w[k] = a ? ld_tag(a, acq) : 0ull;
         }
 #pragma unroll
         for (int k = 0; k < STAGE_BATCH; k++) {
-            const uint32_t i = i0 + k * CG_THREADS;
-            if (i < n && ok) {
+            const uint32_t v = v0 + k * CG_THREADS;
+            const unsigned long long* a = v < nvirt ? addr(v) : nullptr;
+            if (a && ok) {
                 if ((uint32_t)(w[k] >> 32) != tag) {
-                    const uint32_t at = per ? (i / per) * 16u + i % per : e0 + i;
-                    w[k] = wait_tag(x + at, tag, st, acq);
+                    w[k] = wait_tag(a, tag, st, acq);
                     ok = (uint32_t)(w[k] >> 32) == tag;
                 }
-                vals[i] = __uint_as_float((uint32_t)w[k]);
+                vals[dst(v)] = __uint_as_float((uint32_t)w[k]);
             }
         }
     }
@@ -182,7 +195,7 @@ __device__ __forceinline__ double df_to_double(Df a) { return (double)a.hi + (do
 
 // One block of 256 threads.  Lists the active chunks by residue (segment li =
 // chunks li, li+256, ... ascending), splits the list into G contiguous ranges
-// of equal weight (liquid cells + 32 per chunk), and reserves this solve's
+// of equal weight (liquid cells + CHUNK_WEIGHT per chunk), and reserves this solve's
 // tag range.  When the 32-bit epoch would wrap, the exchange words are
 // cleared first, so no stale word can carry a tag of a later solve.
 __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
@@ -198,7 +211,7 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
         const uint32_t f = b.chunk_flag[c];
         if (f) {
             cnt++;
-            wsum += f + 32u;
+            wsum += f + CHUNK_WEIGHT;
         }
     }
     uint32_t x = cnt, y = wsum;
@@ -233,7 +246,7 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
         const uint32_t f = b.chunk_flag[c];
         if (!f) continue;
         b.cg_chunk[pos] = c;
-        const uint64_t X1 = X + f + 32u;
+        const uint64_t X1 = X + f + CHUNK_WEIGHT;
         // blocks bb with X*G < bb*W <= X1*G start after this entry
         const uint64_t lo = X * G / W + 1, hi = X1 * G / W;
         for (uint64_t bb = lo; bb <= hi; bb++) start[bb] = pos + 1;
@@ -246,8 +259,10 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
         start[0] = 0;
     __syncthreads();
     // Slot layout: block bb's chunk partials at bb*S + j when every block's
-    // range fits S (a multiple of 16 words, so each block starts a 128-byte
-    // line) and the area holds G*S words; else densely at plan entry s_bb + j.
+    // range fits S (a power of two >= 16 words, so each block starts a
+    // 128-byte line and a slot's block is a shift away) and the area holds G*S
+    // words; else densely at plan entry s_bb + j.  The header keeps log2(S),
+    // 0 for the dense layout.
     uint32_t mmax = 0;
     for (uint32_t bb = li; bb < G; bb += CHUNK) {
         const uint32_t mb = start[bb + 1] - start[bb];
@@ -262,8 +277,10 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
     __syncthreads();
     if (li == 0) {
         for (uint32_t w = 0; w < CHUNK / 32; w++) mmax = s_wc[w] > mmax ? s_wc[w] : mmax;
-        const uint64_t S = (mmax + 15u) & ~15u;
-        hdr[CHUNK + 2] = (A > 0 && A <= VAL_CAP && S * G <= (uint64_t)nchunks + 16u * G) ? (uint32_t)S : 0u;
+        uint32_t lg = 4;
+        while ((1u << lg) < mmax && lg < 31) lg++;
+        const uint64_t S = 1ull << lg;
+        hdr[CHUNK + 2] = (A > 0 && A <= VAL_CAP && S * G <= (uint64_t)nchunks + 16u * G) ? lg : 0u;
     }
     if (li == 0) {
         const uint32_t span = 2u * (P.iters < TAG_SPAN_MAX ? P.iters : TAG_SPAN_MAX) + 4u;
@@ -298,6 +315,9 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     constexpr bool f64 = F64;
     const float tol_sq = P.tol_sq;
     const double tol_sq_d = P.tol_sq_d;
+    // Stopping test enabled: evaluated once (a double compare in the loop
+    // would run on the FP64 pipe in every warp of every iteration).
+    const bool stop_on = F64 ? P.tol_sq_d > 0.0 : P.tol_sq > 0.0f;
     DevStats* st = b.st;
     const uint32_t G = gridDim.x, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     float* __restrict__ r = b.r;
@@ -308,7 +328,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     const uint32_t* hdr = b.cg_off;
     for (uint32_t i = tid; i <= CHUNK; i += CG_THREADS) sh.off[i] = hdr[i];
     const uint32_t tag_base = hdr[CHUNK + 1];
-    const uint32_t S = hdr[CHUNK + 2];  // slot line stride per block, 0 = dense plan order
+    const uint32_t lgS = hdr[CHUNK + 2];  // log2 of the slot stride per block, 0 = dense plan order
+    const uint32_t S = lgS ? 1u << lgS : 0u;
     const uint32_t* bstart = hdr + CHUNK + 3;
     for (uint32_t i = tid; i <= G; i += CG_THREADS) sh.bstart[i] = bstart[i];
     const uint32_t s0 = bstart[blockIdx.x], s1 = bstart[blockIdx.x + 1];
@@ -370,14 +391,15 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         bool ok = true;
         for (uint32_t w0 = 0; w0 < A; w0 += VAL_CAP) {
             const uint32_t wn = A - w0 < VAL_CAP ? A - w0 : VAL_CAP;
-            if (x && S) {  // one window (A <= VAL_CAP): walk the blocks' lines
+            if (x && S) {  // one window (A <= VAL_CAP): walk the blocks' lines.  Written
+                           // out rather than through stage_words: measured 0.5 ms/step faster.
                 for (uint32_t v0 = tid; v0 < G * S; v0 += STAGE_BATCH * CG_THREADS) {
                     unsigned long long w[STAGE_BATCH];
                     uint32_t dst[STAGE_BATCH];
 #pragma unroll
                     for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
                         const uint32_t v = v0 + k2 * CG_THREADS;
-                        const uint32_t bb = v / S, j = v - bb * S;
+                        const uint32_t bb = v >> lgS, j = v & (S - 1u);
                         const bool use = v < G * S && j < sh.bstart[bb + 1] - sh.bstart[bb];
                         dst[k2] = use ? sh.bstart[bb] + j : 0xffffffffu;
                         w[k2] = use ? ld_tag(x + v, acq) : 0ull;
@@ -393,8 +415,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         }
                     }
                 }
-            } else if (x) {
-                ok = stage_tagged(x, w0, wn, tag, sh.vals, st, acq);
+            } else if (x) {  // plan order, window [w0, w0 + wn)
+                ok = stage_words(
+                    wn, tag, acq, st, sh.vals, [&](uint32_t v) -> const unsigned long long* { return x + w0 + v; },
+                    [&](uint32_t v) -> uint32_t { return v; });
             } else {
                 for (uint32_t i = tid; i < wn; i += CG_THREADS) sh.vals[i] = b.part_rr[plan[w0 + i]];
             }
@@ -423,7 +447,10 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // at 16*b), summed by every warp in the same fixed order (lanes stride
     // over blocks, then a shuffle tree), so no broadcast is needed.
     auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, Df& out) -> bool {
-        const bool ok = stage_tagged(words, 0, 2 * G, tag, sh.vals, st, acq, 2u);
+        const bool ok = stage_words(
+            2 * G, tag, acq, st, sh.vals,
+            [&](uint32_t v) -> const unsigned long long* { return words + (v >> 1) * 16u + (v & 1u); },
+            [&](uint32_t v) -> uint32_t { return v; });
         if (__syncthreads_or(!ok)) return false;
         Df acc = {0.0f, 0.0f};
         for (uint32_t bb = lane; bb < G; bb += 32) acc = df_add(acc, Df{sh.vals[2 * bb], sh.vals[2 * bb + 1]});
@@ -447,12 +474,12 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             }
         }
     };
-    // Warp w publishes the tree of chunk j0 + w of the pass.
+    // Warp w publishes the trees of chunks j0 + w and j0 + w + 32 of the pass.
     auto publish_trees = [&](uint32_t j0, uint32_t nb, unsigned long long* slots, uint32_t tag, bool rel) {
         __syncthreads();
-        if (warp < nb) {
-            const float v = chunk_tree(sh.tree[warp], lane);
-            if (lane == 0) publish(slots + slot0 + j0 + warp, tag, v, rel);
+        for (uint32_t j = warp; j < nb; j += CG_WARPS) {
+            const float v = chunk_tree(sh.tree[j], lane);
+            if (lane == 0) publish(slots + slot0 + j0 + j, tag, v, rel);
         }
     };
 
@@ -667,13 +694,13 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             if (!reduce_df(wordB, tag, true, rs_new)) return;
             beta = rs_old_d.hi > 1e-30f ? df_div(rs_new, rs_old_d) : 0.0f;
             rs_old_d = rs_new;
-            done = tol_sq_d > 0.0 && df_le(rs_new, thr_d);
+            done = stop_on && df_le(rs_new, thr_d);
         } else {
             float rs_new;
             if (!reduce_f32(slotB, tag, true, rs_new)) return;
             beta = rs_old_f > 1e-30f ? __fdiv_rn(rs_new, rs_old_f) : 0.0f;  // cg_beta.wgsl:16-23
             rs_old_f = rs_new;
-            done = tol_sq > 0.0f && rs_new <= __fmul_rn(tol_sq, rs_init_f);  // cg_beta.wgsl:25-30
+            done = stop_on && rs_new <= __fmul_rn(tol_sq, rs_init_f);  // cg_beta.wgsl:25-30
         }
         if (done) break;
     }

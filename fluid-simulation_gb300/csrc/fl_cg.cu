@@ -66,7 +66,10 @@ struct CgShared {
     float seg[CHUNK];          // segment sums (cg_reduce_final.wgsl thread accumulators)
     float red[2 * CG_WARPS];   // float-float warp partials
     uint32_t wcnt[CG_WARPS];
+    uint32_t layout, nslot;              // exchange slot layout (0 plan order, 1 lines, 2 one line per block), slots used
     uint32_t bstart[MAX_CG_BLOCKS + 1];  // first plan entry of every block
+    uint32_t spos[MAX_CG_BLOCKS + 1];    // first exchange slot of every block
+    uint16_t lineblk[VAL_CAP / 16 + MAX_CG_BLOCKS];  // line of the slot area -> owning block
 };
 static_assert(sizeof(CgShared) <= 227 * 1024, "CG shared memory exceeds the 227 KB per-block limit");
 
@@ -76,9 +79,12 @@ static_assert(sizeof(CgShared) <= 227 * 1024, "CG shared memory exceeds the 227 
 __device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
     asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+// The polling loads carry no "memory" clobber, so the compiler may compute
+// all of a batch's addresses (shared-memory lookups) before issuing the
+// loads; what follows a poll is ordered by data dependence or a barrier.
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
     unsigned long long v;
-    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
     return v;
 }
 __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned long long v) {
@@ -86,7 +92,7 @@ __device__ __forceinline__ void st_relaxed_u64(unsigned long long* p, unsigned l
 }
 __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
     unsigned long long v;
-    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p));
     return v;
 }
 // `rel`: release store, for the exchange after which other blocks read this
@@ -206,6 +212,7 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
     const uint32_t li = threadIdx.x, lane = li & 31, warp = li >> 5;
     uint32_t* hdr = b.cg_off;
     uint32_t* start = hdr + CHUNK + 3;
+    uint32_t* spos = start + G + 1;
     uint32_t cnt = 0, wsum = 0;
     for (uint32_t c = li; c < nchunks; c += CHUNK) {
         const uint32_t f = b.chunk_flag[c];
@@ -258,30 +265,47 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
     else if (li == 0)
         start[0] = 0;
     __syncthreads();
-    // Slot layout: block bb's chunk partials at bb*S + j when every block's
-    // range fits S (a power of two >= 16 words, so each block starts a
-    // 128-byte line and a slot's block is a shift away) and the area holds G*S
-    // words; else densely at plan entry s_bb + j.  The header keeps log2(S),
-    // 0 for the dense layout.
-    uint32_t mmax = 0;
+    // Slot layout: block bb's chunk partials at spos[bb] + j, each block's
+    // range rounded up to whole 128-byte lines (16 words) and packed in block
+    // order (a reader maps a line back to its block); used when all chunk
+    // partials fit one staging window.  Else densely at plan entry s_bb + j
+    // (spos[bb] = s_bb).  hdr[CHUNK + 2] = 1 for the line layout.
+    const bool lines = A > 0 && A <= VAL_CAP;
+    {
+        const uint32_t per = (G + CHUNK - 1) / CHUNK;
+        const uint32_t b0 = li * per < G ? li * per : G, b1 = b0 + per < G ? b0 + per : G;
+        uint32_t mine = 0;
+        for (uint32_t bb = b0; bb < b1; bb++) {
+            const uint32_t mb = start[bb + 1] - start[bb];
+            mine += lines ? (mb + 15u) & ~15u : mb;
+        }
+        uint32_t xs = mine;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, xs, o);
+            if (lane >= (uint32_t)o) xs += t;
+        }
+        if (lane == 31) s_wc[warp] = xs;
+        __syncthreads();
+        uint32_t run = xs - mine;
+        for (uint32_t w = 0; w < warp; w++) run += s_wc[w];
+        for (uint32_t bb = b0; bb < b1; bb++) {
+            spos[bb] = run;
+            const uint32_t mb = start[bb + 1] - start[bb];
+            run += lines ? (mb + 15u) & ~15u : mb;
+        }
+        if (b0 < b1 && b1 == G) spos[G] = run;
+        if (G == 0 && li == 0) spos[0] = 0;
+    }
+    // 2: every block owns 1..16 chunks, so block bb's line is simply line bb
+    uint32_t mmin = 0xffffffffu, mmax = 0;
     for (uint32_t bb = li; bb < G; bb += CHUNK) {
         const uint32_t mb = start[bb + 1] - start[bb];
+        mmin = mb < mmin ? mb : mmin;
         mmax = mb > mmax ? mb : mmax;
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const uint32_t v = __shfl_xor_sync(0xffffffffu, mmax, o);
-        mmax = v > mmax ? v : mmax;
-    }
-    if (lane == 0) s_wc[warp] = mmax;
-    __syncthreads();
-    if (li == 0) {
-        for (uint32_t w = 0; w < CHUNK / 32; w++) mmax = s_wc[w] > mmax ? s_wc[w] : mmax;
-        uint32_t lg = 4;
-        while ((1u << lg) < mmax && lg < 31) lg++;
-        const uint64_t S = 1ull << lg;
-        hdr[CHUNK + 2] = (A > 0 && A <= VAL_CAP && S * G <= (uint64_t)nchunks + 16u * G) ? lg : 0u;
-    }
+    const int one_line = __syncthreads_and(mmin >= 1u && mmax <= 16u);
+    if (li == 0) hdr[CHUNK + 2] = lines ? (one_line ? 2u : 1u) : 0u;
     if (li == 0) {
         const uint32_t span = 2u * (P.iters < TAG_SPAN_MAX ? P.iters : TAG_SPAN_MAX) + 4u;
         uint32_t e0 = (uint32_t)b.cg_x[0];
@@ -328,13 +352,24 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     const uint32_t* hdr = b.cg_off;
     for (uint32_t i = tid; i <= CHUNK; i += CG_THREADS) sh.off[i] = hdr[i];
     const uint32_t tag_base = hdr[CHUNK + 1];
-    const uint32_t lgS = hdr[CHUNK + 2];  // log2 of the slot stride per block, 0 = dense plan order
-    const uint32_t S = lgS ? 1u << lgS : 0u;
+    // Block-uniform values read only by the exchanges live in shared memory
+    // (sh.layout, sh.nslot, sh.off[CHUNK]) rather than in registers: the cell
+    // loops are at the 64-register limit of a 1024-thread block.
+    if (tid == 0) sh.layout = hdr[CHUNK + 2];
     const uint32_t* bstart = hdr + CHUNK + 3;
-    for (uint32_t i = tid; i <= G; i += CG_THREADS) sh.bstart[i] = bstart[i];
+    const uint32_t* spos = bstart + G + 1;
+    for (uint32_t i = tid; i <= G; i += CG_THREADS) {
+        sh.bstart[i] = bstart[i];
+        sh.spos[i] = spos[i];
+    }
     const uint32_t s0 = bstart[blockIdx.x], s1 = bstart[blockIdx.x + 1];
     const uint32_t m = s1 - s0;  // this block's chunks: plan entries [s0, s1)
-    const uint32_t slot0 = S ? blockIdx.x * S : s0;  // this block's first slot
+    const uint32_t slot0 = spos[blockIdx.x];  // this block's first slot
+    if (tid == 0) sh.nslot = spos[G];
+    __syncthreads();
+    if (sh.layout != 0u)  // line -> owning block
+        for (uint32_t bb = tid; bb < G; bb += CG_THREADS)
+            for (uint32_t L = sh.spos[bb] >> 4; L < sh.spos[bb + 1] >> 4; L++) sh.lineblk[L] = (uint16_t)bb;
     const size_t nslot = (size_t)nchunks + 16 * (size_t)G;
     unsigned long long* slotA = b.cg_x + 8;        // d.q chunk partials
     unsigned long long* slotB = slotA + nslot;     // r.r chunk partials
@@ -389,18 +424,22 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     auto reduce_f32 = [&](const unsigned long long* x, uint32_t tag, bool acq, float& out) -> bool {
         float acc = 0.0f;
         bool ok = true;
+        const uint32_t A = sh.off[CHUNK];
         for (uint32_t w0 = 0; w0 < A; w0 += VAL_CAP) {
             const uint32_t wn = A - w0 < VAL_CAP ? A - w0 : VAL_CAP;
-            if (x && S) {  // one window (A <= VAL_CAP): walk the blocks' lines.  Written
-                           // out rather than through stage_words: measured 0.5 ms/step faster.
-                for (uint32_t v0 = tid; v0 < G * S; v0 += STAGE_BATCH * CG_THREADS) {
+            if (x && sh.layout != 0u) {  // one window (A <= VAL_CAP): walk the blocks' lines.  Written
+                                         // out rather than through stage_words: measured 0.5 ms/step faster.
+                const uint32_t nslot_used = sh.nslot;
+                const bool one_line = sh.layout == 2u;
+                for (uint32_t v0 = tid; v0 < nslot_used; v0 += STAGE_BATCH * CG_THREADS) {
                     unsigned long long w[STAGE_BATCH];
                     uint32_t dst[STAGE_BATCH];
 #pragma unroll
                     for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
                         const uint32_t v = v0 + k2 * CG_THREADS;
-                        const uint32_t bb = v >> lgS, j = v & (S - 1u);
-                        const bool use = v < G * S && j < sh.bstart[bb + 1] - sh.bstart[bb];
+                        const uint32_t bb = v < nslot_used ? (one_line ? v >> 4 : (uint32_t)sh.lineblk[v >> 4]) : 0u;
+                        const uint32_t j = v - sh.spos[bb];
+                        const bool use = v < nslot_used && j < sh.bstart[bb + 1] - sh.bstart[bb];
                         dst[k2] = use ? sh.bstart[bb] + j : 0xffffffffu;
                         w[k2] = use ? ld_tag(x + v, acq) : 0ull;
                     }

@@ -87,8 +87,8 @@ struct DevBufs {
     uint32_t* cg_chunk;    // CG plan: active chunks grouped by (chunk mod 256), ascending
     uint32_t* cg_off;      // CG plan header, cg_plan_words(max blocks) words: 257 segment
                            // offsets into cg_chunk, the launch's tag base, the slot
-                           // line stride, then the first plan entry of every block
-                           // (blocks + 1 entries)
+                           // layout, the first plan entry of every block and the
+                           // first exchange slot of every block (blocks + 1 each)
     unsigned long long* cg_x;  // CG exchange words, cg_x_words(nchunks, max blocks): [0] tag
                                // epoch (persists across solves), then tagged partials
 };
@@ -99,7 +99,7 @@ struct DevBufs {
 #else
 #define FL_HD
 #endif
-FL_HD constexpr size_t cg_plan_words(size_t max_blocks) { return (size_t)CHUNK + 3 + max_blocks + 1; }
+FL_HD constexpr size_t cg_plan_words(size_t max_blocks) { return (size_t)CHUNK + 3 + 2 * (max_blocks + 1); }
 FL_HD constexpr size_t cg_x_words(size_t nchunks, size_t max_blocks) { return 8 + 2 * nchunks + 64 * max_blocks; }
 
 // Buffers of one adjoint step (fl_adjoint.cu).

@@ -44,6 +44,10 @@ __global__ void __launch_bounds__(256) k_classify(DevBufs b, uint32_t C) {
 // ---------------------------------------------------------------------------
 // P2G
 
+// k_p2g_tile: one 256-thread block per 8^3 tile of cells.  The tile's halo box
+// (one cell around it) is a set of (y, z) rows, each a contiguous range of the
+// sorted bins; the block flattens them into one index space (row prefix sums
+// in shared memory) so every thread keeps P2G_BATCH particle loads in flight.
 struct TileGeom {
     int x0, y0, z0;     // first cell of the tile
     int xe, ye, ze;     // one past the last cell of the tile
@@ -100,9 +104,15 @@ __device__ __forceinline__ void p2g_component(const DevParams& P, const TileGeom
     }
 }
 
+constexpr int P2G_ROWS = (TILE + 2) * (TILE + 2);  // halo rows (y, z) of a tile
+constexpr int P2G_BATCH = 4;                        // particles in flight per thread
+
 __global__ void __launch_bounds__(256) k_p2g_tile(DevBufs b, int tiles_x, int tiles_y) {
     __shared__ int32_t s_num[3][TS_U];
     __shared__ int32_t s_den[3][TS_U];
+    __shared__ uint32_t s_row_beg[P2G_ROWS];      // first sorted particle of each halo row
+    __shared__ uint32_t s_row_off[P2G_ROWS + 1];  // prefix of the row lengths
+    __shared__ uint32_t s_wsum[4];
     const DevParams& P = *b.prm;
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
     const int tid = blockIdx.x;
@@ -115,32 +125,78 @@ __global__ void __launch_bounds__(256) k_p2g_tile(DevBufs b, int tiles_x, int ti
         (&s_num[0][0])[i] = 0;
         (&s_den[0][0])[i] = 0;
     }
-    __syncthreads();
 
     // Halo of one cell: every non-stray particle whose taps reach an owned face
     // has its bin in [x0-1, xe] x [y0-1, ye] x [z0-1, ze] (clamped to the grid).
+    // Each (y, z) row of that box is one contiguous range of the sorted bins.
     const int hx0 = max(T.x0 - 1, 0), hx1 = min(T.xe, nx - 1);
     const int hy0 = max(T.y0 - 1, 0), hy1 = min(T.ye, ny - 1);
     const int hz0 = max(T.z0 - 1, 0), hz1 = min(T.ze, nz - 1);
     const int rows_y = hy1 - hy0 + 1, rows = rows_y * (hz1 - hz0 + 1);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const float inv_h = P.inv_h;
-    const float o0 = P.origin[0], o1 = P.origin[1], o2 = P.origin[2];
-    for (int row = warp; row < rows; row += nwarps) {
-        const int cy = hy0 + row % rows_y, cz = hz0 + row / rows_y;
+    uint32_t len = 0;
+    if ((int)threadIdx.x < rows) {
+        const int cy = hy0 + (int)threadIdx.x % rows_y, cz = hz0 + (int)threadIdx.x / rows_y;
         const uint32_t c0 = (uint32_t)hx0 + P.nx * ((uint32_t)cy + P.ny * (uint32_t)cz);
         const uint32_t c1 = c0 + (uint32_t)(hx1 - hx0);
         const uint32_t pbeg = b.offsets[c0];
-        const uint32_t pend = b.offsets[c1] + b.counts[c1];
-        for (uint32_t pp = pbeg + lane; pp < pend; pp += 32) {
-            const float4 pos = b.part_sorted[2 * (size_t)pp];
-            if (pos.w != 0.0f) continue;  // stray: handled by k_p2g_strays
-            const float4 vel = b.part_sorted[2 * (size_t)pp + 1];
-            const float q[3] = {__fmul_rn(__fsub_rn(pos.x, o0), inv_h), __fmul_rn(__fsub_rn(pos.y, o1), inv_h),
-                                __fmul_rn(__fsub_rn(pos.z, o2), inv_h)};
-            p2g_component(P, T, 0, q, vel.x, s_num[0], s_den[0]);
-            p2g_component(P, T, 1, q, vel.y, s_num[1], s_den[1]);
-            p2g_component(P, T, 2, q, vel.z, s_num[2], s_den[2]);
+        len = b.offsets[c1] + b.counts[c1] - pbeg;
+        s_row_beg[threadIdx.x] = pbeg;
+    }
+    // exclusive prefix of the row lengths (rows <= 100 < 128: warps 0..3)
+    {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t x = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (warp < 4 && lane == 31) s_wsum[warp] = x;
+        __syncthreads();
+        if ((int)threadIdx.x < rows) {
+            uint32_t base = 0;
+            for (int w = 0; w < warp; w++) base += s_wsum[w];
+            s_row_off[threadIdx.x] = base + x - len;
+        }
+        if (threadIdx.x == 0) s_row_off[rows] = s_wsum[0] + s_wsum[1] + s_wsum[2] + s_wsum[3];
+        __syncthreads();
+    }
+    const uint32_t total = s_row_off[rows];
+    const float inv_h = P.inv_h;
+    const float o0 = P.origin[0], o1 = P.origin[1], o2 = P.origin[2];
+    // Flattened particle index f of the tile's halo box.  Within each group of
+    // 256 indices thread t takes (t % 32) * 8 + t / 32, so the lanes of a warp
+    // hold particles of different cells (8 per cell when dense) and their
+    // shared-memory atomics rarely meet on one face.
+    const uint32_t swz = (threadIdx.x & 31u) * 8u + (threadIdx.x >> 5);
+    for (uint32_t g0 = 0; g0 < total; g0 += 256u * P2G_BATCH) {
+        float4 pos[P2G_BATCH], vel[P2G_BATCH];
+        bool use[P2G_BATCH];
+#pragma unroll
+        for (int k = 0; k < P2G_BATCH; k++) {
+            const uint32_t f = g0 + 256u * k + swz;
+            use[k] = f < total;
+            uint32_t pp = 0;
+            if (use[k]) {
+                int lo = 0, hi = rows - 1;  // last row with s_row_off[row] <= f
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (s_row_off[mid] <= f) lo = mid;
+                    else hi = mid - 1;
+                }
+                pp = s_row_beg[lo] + (f - s_row_off[lo]);
+            }
+            pos[k] = use[k] ? b.part_sorted[2 * (size_t)pp] : make_float4(0.f, 0.f, 0.f, 1.f);
+            vel[k] = use[k] ? b.part_sorted[2 * (size_t)pp + 1] : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+#pragma unroll
+        for (int k = 0; k < P2G_BATCH; k++) {
+            if (!use[k] || pos[k].w != 0.0f) continue;  // stray: handled by k_p2g_strays
+            const float q[3] = {__fmul_rn(__fsub_rn(pos[k].x, o0), inv_h), __fmul_rn(__fsub_rn(pos[k].y, o1), inv_h),
+                                __fmul_rn(__fsub_rn(pos[k].z, o2), inv_h)};
+            p2g_component(P, T, 0, q, vel[k].x, s_num[0], s_den[0]);
+            p2g_component(P, T, 1, q, vel[k].y, s_num[1], s_den[1]);
+            p2g_component(P, T, 2, q, vel[k].z, s_num[2], s_den[2]);
         }
     }
     __syncthreads();

@@ -47,6 +47,7 @@ typedef struct orc_handle_f64 orc_handle_f64;
     int orc_add_velocity_d##SFX(orc_handle##SFX* h, const double* dv, double eps);               \
     int orc_mean_position_d##SFX(orc_handle##SFX* h, double out[3]);                             \
     int orc_add_position_d##SFX(orc_handle##SFX* h, const double* dx, double eps);               \
+    int orc_set_pressure##SFX(orc_handle##SFX* h, const float* p);                               \
     int orc_solve_pressure##SFX(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* ct,        \
                                 const float* div, const float* p_in, float* p_out, float h,      \
                                 float rho, float dt, uint32_t max_iters, uint32_t warm,          \

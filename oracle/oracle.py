@@ -59,6 +59,7 @@ def load(build=True):
             "orc_get_divergence": [ctypes.c_void_p, _fp],
             "orc_set_gravity_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)],
             "orc_add_velocity_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_double],
+            "orc_set_pressure": [ctypes.c_void_p, _fp],
             "orc_mean_position_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)],
             "orc_add_position_d": [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_double],
             "orc_solve_pressure": [_u32, _u32, _u32, _u8p_t, _fp, _fp, _fp, ctypes.c_float, ctypes.c_float,
@@ -211,6 +212,11 @@ class OracleFluid:
     def add_position_d(self, dx, eps):
         a = np.ascontiguousarray(dx, np.float64).reshape(-1, 3)
         self._c(self._f("orc_add_position_d")(self.h, a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), eps))
+
+    def set_pressure(self, p):
+        """Warm-start pressure of the next step (precision-study hook)."""
+        a = np.ascontiguousarray(p, np.float32)
+        self._c(self._f("orc_set_pressure")(self.h, f32p(a)))
 
     def mean_position_d(self):
         out = np.zeros(3, np.float64)

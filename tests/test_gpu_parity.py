@@ -296,3 +296,18 @@ def test_128_grid_one_step_bit_exact(lib, oracle):
     g.step(1)
     o.step(1)
     assert_same_state(g, o, "128^3 step 0")
+
+
+def test_256_grid_two_steps_bit_exact(lib, oracle):
+    """The 256^3, 18.8M-particle block: its CG holds more active chunks than one
+    staging window (plan-order exchange slots, windowed reduction) and more
+    liquid cells per block than the shared-memory cell list (the unlisted-cell
+    path) — both bit-exact against the oracle."""
+    p, parts, _ = scenes.workload("block256")
+    g, o = make_pair(oracle, p, parts)
+    for s in range(2):
+        g.step(1)
+        o.step(1)
+        assert_same_state(g, o, "256^3 step %d" % s)
+    g.close()
+    o.close()

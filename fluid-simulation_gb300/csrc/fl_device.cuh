@@ -9,6 +9,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/fluidgb.h"
+
 namespace fl {
 
 constexpr uint8_t CELL_SOLID = 0, CELL_LIQUID = 1, CELL_AIR = 2;
@@ -256,6 +258,24 @@ cudaError_t launch_iota(uint32_t* ids, uint32_t n, cudaStream_t s);
 cudaError_t launch_impulse(float4* part, const DevParams* prm, float dx, float dy, float dz,
                            const LaunchCfg& L, cudaStream_t s);
 int cg_max_blocks_per_sm();
+cudaError_t launch_slice(const DevBufs& b, uint32_t nx, uint32_t ny, uint32_t mode, uint32_t k, float4* out,
+                         cudaStream_t s);
+// Particle seeding (fl_scene.cu): one liquid block of the jittered lattice.
+struct SeedBlock {
+    float wmin[3];      // world position of the block's min corner
+    float spacing;      // lattice spacing
+    int32_t counts[3];  // lattice points per axis
+    uint32_t first;     // index of the block's first particle
+};
+struct SeedArgs {
+    SeedBlock blk[16];  // FL_SCENE_MAX_BLOCKS
+    uint32_t nblocks, n;
+    float lo[3], hi[3];  // wall clamp of the positions
+};
+// Layout of generate_particles for the settings' tank; the total count, or -1.
+long long seed_layout(const fl_params& prm, const fl_block* blocks, uint32_t nblocks, uint32_t particle_count,
+                      SeedArgs* out);
+cudaError_t launch_seed(const SeedArgs& a, float4* part, cudaStream_t s);
 struct AdjBufs;
 cudaError_t launch_adj_g2p(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s);

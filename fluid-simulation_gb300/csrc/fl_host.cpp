@@ -50,6 +50,7 @@ struct fl_handle {
     std::vector<float> init_part;
     uint32_t init_n = 0;
     uint64_t substeps = 0;
+    float4* slice_buf = nullptr;  // device staging of fl_grid_slice (nx*ny float4), allocated on first use
     std::string err;
 };
 
@@ -416,6 +417,7 @@ fl_status fl_destroy(fl_handle* h) {
         if (h->ev[k]) cudaEventDestroy(h->ev[k]);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     if (h->pool) cudaFree(h->pool);
+    if (h->slice_buf) cudaFree(h->slice_buf);
     delete h;
     return FL_OK;
 }
@@ -859,6 +861,66 @@ fl_status fl_set_particles_device(fl_handle* h, const void* src_dev, uint32_t n)
         fl_status s = upload_params(h);
         if (s != FL_OK) return s;
     }
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    return FL_OK;
+}
+
+fl_status fl_seed_count(const fl_params* params, const fl_block* blocks, uint32_t nblocks, uint32_t particle_count,
+                        uint32_t* n_out) {
+    if (!params || !n_out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    fl::SeedArgs a;
+    const long long n = fl::seed_layout(*params, blocks, nblocks, particle_count, &a);
+    if (n < 0) return set_err(nullptr, FL_INVALID_ARG, "need 1..FL_SCENE_MAX_BLOCKS blocks");
+    *n_out = (uint32_t)n;
+    return FL_OK;
+}
+
+// generate_particles (fluid.rs:1838-1913) on the device: the lattice is laid
+// out on the host, every particle is computed by its own thread.
+fl_status fl_seed_particles(fl_handle* h, const fl_block* blocks, uint32_t nblocks, uint32_t particle_count,
+                            uint32_t* n_out) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    fl::SeedArgs a;
+    const long long n = fl::seed_layout(h->prm, blocks, nblocks, particle_count, &a);
+    if (n < 0) return set_err(h, FL_INVALID_ARG, "need 1..FL_SCENE_MAX_BLOCKS blocks");
+    if (n_out) *n_out = (uint32_t)n;
+    if ((unsigned long long)n > h->cap)
+        return set_err(h, FL_INVALID_ARG, "the layout has " + std::to_string(n) + " particles, above the capacity");
+    FL_CUDA(h, fl::launch_seed(a, h->partA, h->stream));
+    // the seeded particles become the state fl_reset restores
+    h->init_part.resize((size_t)n * 8);
+    if (n) FL_CUDA(h, cudaMemcpyAsync(h->init_part.data(), h->partA, (size_t)n * 32, cudaMemcpyDeviceToHost, h->stream));
+    FL_CUDA(h, cudaStreamSynchronize(h->stream));
+    h->init_n = (uint32_t)n;
+    return fl_reset(h);
+}
+
+// Headless grid slice (slice.wgsl:69-141): one float4 {r, g, b, visible} per
+// cell of the XY cross-section at k.
+fl_status fl_grid_slice_device(fl_handle* h, uint32_t mode, uint32_t slice_k, void* rgba_dev) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (!rgba_dev || ((uintptr_t)rgba_dev & 15u)) return set_err(h, FL_INVALID_ARG, "rgba_dev must be 16-byte aligned");
+    const uint32_t k = slice_k == FL_SLICE_MIDDLE ? h->nz / 2 : slice_k;
+    if (k >= h->nz) return set_err(h, FL_INVALID_ARG, "slice_k out of range");
+    FL_CUDA(h, fl::launch_slice(h->b, h->nx, h->ny, mode, k, (float4*)rgba_dev, h->stream));
+    return FL_OK;
+}
+
+fl_status fl_grid_slice(fl_handle* h, uint32_t mode, uint32_t slice_k, float* rgba_out) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (!rgba_out) return set_err(h, FL_INVALID_ARG, "rgba_out is NULL");
+    const size_t bytes = sizeof(float4) * (size_t)h->nx * h->ny;
+    if (!h->slice_buf) {
+        cudaError_t e = cudaMalloc(&h->slice_buf, bytes);
+        if (e != cudaSuccess) {
+            (void)cudaGetLastError();
+            h->slice_buf = nullptr;
+            return set_err(h, FL_OOM, "slice buffer allocation failed");
+        }
+    }
+    fl_status s = fl_grid_slice_device(h, mode, slice_k, h->slice_buf);
+    if (s != FL_OK) return s;
+    FL_CUDA(h, cudaMemcpyAsync(rgba_out, h->slice_buf, bytes, cudaMemcpyDeviceToHost, h->stream));
     FL_CUDA(h, cudaStreamSynchronize(h->stream));
     return FL_OK;
 }

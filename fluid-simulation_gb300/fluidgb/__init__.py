@@ -5,11 +5,11 @@ this package is the ctypes binding plus seeded scene generators.
 """
 from ._abi import (FL_CELL_AIR, FL_CELL_LIQUID, FL_CELL_SOLID, FL_CG_F32, FL_CG_F64, FL_INVALID_ARG, FL_OK,
                    FL_TIMEOUT, FlGridView, FlParams, FlStats, Fluid, FluidError, LIB_PATH, SIGNATURES,
-                   default_params, face_counts, load_library, solve_pressure)
+                   Timestep, default_params, face_counts, load_library, solve_pressure)
 from . import scenes
 
 __all__ = [
     "FL_CELL_AIR", "FL_CELL_LIQUID", "FL_CELL_SOLID", "FL_CG_F32", "FL_CG_F64", "FL_INVALID_ARG", "FL_OK",
     "FL_TIMEOUT", "FlGridView", "FlParams", "FlStats", "Fluid", "FluidError", "LIB_PATH", "SIGNATURES",
-    "default_params", "face_counts", "load_library", "solve_pressure", "scenes",
+    "Timestep", "default_params", "face_counts", "load_library", "solve_pressure", "scenes",
 ]

@@ -65,6 +65,27 @@ class FlGridView(ctypes.Structure):
 
 assert ctypes.sizeof(FlParams) == 160
 
+FL_POLICY_FIXED_DROP_CAP, FL_POLICY_EXPLICIT_EXPORT = 0, 1
+FL_PRESET_FALLING_BLOB, FL_PRESET_DAM_BREAK, FL_PRESET_DOUBLE_SPLASH = 0, 1, 2
+
+
+class FlBlock(ctypes.Structure):
+    """A liquid block in normalized tank space (scene/mod.rs LiquidBlock)."""
+    _fields_ = [("min", c_f32 * 3), ("max", c_f32 * 3)]
+
+
+class FlTimestepStats(ctypes.Structure):
+    """TimestepFrameStats (timestep.rs:21-50)."""
+    _fields_ = [
+        ("substeps", c_u32), ("natural_substeps", c_u32), ("max_substeps", c_u32), ("substep_cap_hit", c_u32),
+        ("fixed_dt", c_f32), ("accumulated_before", c_f32), ("accumulated_after", c_f32),
+        ("dropped_this_frame", c_f32), ("sim_advanced", c_f32), ("wall_dt", c_f32), ("sim_time_scale", c_f32),
+        ("real_time_factor", c_f32), ("policy", c_u32),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "fl_abi_version": (c_u32, []),
@@ -113,6 +134,30 @@ SIGNATURES = {
     "fl_step_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _fp, c_u32,
                                        c_f32]),
     "fl_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "fl_scene_blocks": (ctypes.c_int, [c_u32, c_f32, c_f32, ctypes.POINTER(FlBlock), ctypes.POINTER(c_u32)]),
+    "fl_scene_seeded_fraction": (ctypes.c_int, [ctypes.POINTER(FlBlock), c_u32, ctypes.POINTER(c_f32)]),
+    "fl_scene_particle_count": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.POINTER(FlBlock), c_u32, c_f32, c_u32,
+                                               ctypes.POINTER(c_u32)]),
+    "fl_seed_count": (ctypes.c_int, [ctypes.POINTER(FlParams), ctypes.POINTER(FlBlock), c_u32, c_u32,
+                                     ctypes.POINTER(c_u32)]),
+    "fl_seed_particles": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlBlock), c_u32, c_u32,
+                                         ctypes.POINTER(c_u32)]),
+    "fl_grid_slice": (ctypes.c_int, [ctypes.c_void_p, c_u32, c_u32, _fp]),
+    "fl_grid_slice_device": (ctypes.c_int, [ctypes.c_void_p, c_u32, c_u32, ctypes.c_void_p]),
+    "fl_timestep_create": (ctypes.c_int, [c_f32, c_u32, ctypes.POINTER(ctypes.c_void_p)]),
+    "fl_timestep_free": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_timestep_steps_for_frame": (ctypes.c_int, [ctypes.c_void_p, c_f32, c_f32, ctypes.POINTER(c_u32)]),
+    "fl_timestep_record_manual_steps": (ctypes.c_int, [ctypes.c_void_p, c_f32, c_u32, c_f32]),
+    "fl_timestep_record_export_steps": (ctypes.c_int, [ctypes.c_void_p, c_f32, c_u32]),
+    "fl_timestep_record_idle_frame": (ctypes.c_int, [ctypes.c_void_p, c_f32, c_f32]),
+    "fl_timestep_reset": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_timestep_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlTimestepStats)]),
+    "fl_timestep_total_dropped": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_f32)]),
+    "fl_timestep_accumulator": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_f32)]),
+    "fl_timestep_policy_label": (ctypes.c_char_p, [c_u32]),
+    "fl_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, c_f32, ctypes.c_int,
+                                ctypes.POINTER(c_u32), ctypes.POINTER(c_u32)]),
+    "fl_export_frame": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32, ctypes.c_double]),
 }
 
 # FL_STAGE_* order (include/fluidgb.h)
@@ -288,6 +333,21 @@ class Fluid:
         self._c(self.lib.fl_get_grid(self.h, ctypes.byref(v)))
         return g
 
+    def seed(self, blocks, particle_count):
+        """generate_particles on the device into this handle; returns the count."""
+        arr = (FlBlock * len(blocks))(*blocks)
+        n = c_u32()
+        self._c(self.lib.fl_seed_particles(self.h, arr, len(blocks), particle_count, ctypes.byref(n)))
+        return n.value
+
+    def grid_slice(self, mode=0, k=None):
+        """(ny, nx, 4) float32 image {r, g, b, visible} of the XY slice at k
+        (default nz/2), the reference slice renderer's per-cell colours."""
+        nx, ny, _ = self.params.grid
+        out = np.empty((ny, nx, 4), np.float32)
+        self._c(self.lib.fl_grid_slice(self.h, mode, 0xFFFFFFFF if k is None else k, _f32p(out)))
+        return out
+
     def get_bins(self):
         n = self.particle_count()
         counts = np.empty(self.C, np.uint32)
@@ -393,3 +453,105 @@ class Tape:
         self.fluid._c(self.fluid.lib.fl_step_adjoint(self.fluid.h, self.t, ctypes.c_void_p(g_out_ptr),
                                                      ctypes.c_void_p(g_in_ptr), gg, cg_iters, cg_tol))
         return [gg[0], gg[1], gg[2]]
+
+
+class Timestep:
+    """Fixed-timestep accumulator (the reference's TimestepController,
+    timestep.rs:64-233) through the C ABI; host only."""
+
+    def __init__(self, fixed_dt, max_substeps, lib=None):
+        self.lib = lib or load_library()
+        h = ctypes.c_void_p()
+        _check(self.lib, self.lib.fl_timestep_create(c_f32(fixed_dt), max_substeps, ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.fl_timestep_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def steps_for_frame(self, render_dt_s, sim_time_scale=1.0):
+        n = c_u32()
+        _check(self.lib, self.lib.fl_timestep_steps_for_frame(self.h, render_dt_s, sim_time_scale, ctypes.byref(n)))
+        return n.value
+
+    def record_manual_steps(self, render_dt_s, substeps, sim_time_scale=1.0):
+        _check(self.lib, self.lib.fl_timestep_record_manual_steps(self.h, render_dt_s, substeps, sim_time_scale))
+
+    def record_export_steps(self, sim_dt_s, substeps):
+        _check(self.lib, self.lib.fl_timestep_record_export_steps(self.h, sim_dt_s, substeps))
+
+    def record_idle_frame(self, render_dt_s, sim_time_scale=1.0):
+        _check(self.lib, self.lib.fl_timestep_record_idle_frame(self.h, render_dt_s, sim_time_scale))
+
+    def reset(self):
+        _check(self.lib, self.lib.fl_timestep_reset(self.h))
+
+    def last_stats(self):
+        s = FlTimestepStats()
+        _check(self.lib, self.lib.fl_timestep_last_stats(self.h, ctypes.byref(s)))
+        d = s.as_dict()
+        d["policy_label"] = self.lib.fl_timestep_policy_label(s.policy).decode()
+        return d
+
+    def total_dropped(self):
+        v = c_f32()
+        _check(self.lib, self.lib.fl_timestep_total_dropped(self.h, ctypes.byref(v)))
+        return v.value
+
+    def accumulator(self):
+        v = c_f32()
+        _check(self.lib, self.lib.fl_timestep_accumulator(self.h, ctypes.byref(v)))
+        return v.value
+
+    def frame(self, fluid, render_dt_ms, sim_speed=1.0, paused=False, pending_steps=0):
+        """FluidApp::frame on `fluid`: returns (substeps run, pending steps left)."""
+        pend = c_u32(pending_steps)
+        n = c_u32()
+        _check(self.lib, self.lib.fl_frame(fluid.h, self.h, render_dt_ms, sim_speed, 1 if paused else 0,
+                                           ctypes.byref(pend), ctypes.byref(n)))
+        return n.value, pend.value
+
+    def export_frame(self, fluid, substeps, sim_dt_s):
+        _check(self.lib, self.lib.fl_export_frame(fluid.h, self.h, substeps, sim_dt_s))
+
+
+def scene_blocks(preset, drop_height=0.72, fill_level=0.2, lib=None):
+    """preset_blocks (scene/mod.rs:204-236) as a list of FlBlock."""
+    lib = lib or load_library()
+    out = (FlBlock * 2)()
+    n = c_u32()
+    _check(lib, lib.fl_scene_blocks(preset, drop_height, fill_level, out, ctypes.byref(n)))
+    return [out[i] for i in range(n.value)]
+
+
+def seeded_fraction(blocks, lib=None):
+    lib = lib or load_library()
+    arr = (FlBlock * max(len(blocks), 1))(*blocks)
+    v = c_f32()
+    _check(lib, lib.fl_scene_seeded_fraction(arr, len(blocks), ctypes.byref(v)))
+    return v.value
+
+
+def scene_particle_count(dims, blocks, density, override_count=0, lib=None):
+    lib = lib or load_library()
+    arr = (FlBlock * max(len(blocks), 1))(*blocks)
+    v = c_u32()
+    _check(lib, lib.fl_scene_particle_count(dims[0], dims[1], dims[2], arr, len(blocks), density, override_count,
+                                            ctypes.byref(v)))
+    return v.value
+
+
+def seed_count(params, blocks, particle_count, lib=None):
+    lib = lib or load_library()
+    arr = (FlBlock * len(blocks))(*blocks)
+    v = c_u32()
+    _check(lib, lib.fl_seed_count(ctypes.byref(params), arr, len(blocks), particle_count, ctypes.byref(v)))
+    return v.value
+

@@ -51,7 +51,9 @@ enum { FL_CELL_SOLID = 0, FL_CELL_LIQUID = 1, FL_CELL_AIR = 2 };
 /* CG inner-product precision (extension field `cg_precision`). */
 enum {
     FL_CG_F32 = 0, /* reference arithmetic: f32 two-level 256-wide tree dots (cg_reduce.wgsl) */
-    FL_CG_F64 = 1  /* f64 inner products, residual norm and convergence test */
+    FL_CG_F64 = 1  /* extended-precision inner products, residual norm and convergence
+                      test (float-float, ~48-bit significand; the FP32 vector arithmetic
+                      is unchanged) */
 };
 
 /*
@@ -231,6 +233,101 @@ fl_status fl_set_profiling(fl_handle* h, int enable);
 /* ms_out[FL_STAGE_COUNT]: summed milliseconds; substeps_out: substeps timed. */
 fl_status fl_get_stage_times(fl_handle* h, double* ms_out, uint64_t* substeps_out);
 fl_status fl_reset_stage_times(fl_handle* h);
+
+/* ---- scene presets and particle seeding ----
+ * The reference's scene presets (app/crates/fluid-lab/src/scene/mod.rs) and
+ * its initial particle layout (generate_particles, app/crates/fluid-lab/src/
+ * gpu/fluid.rs:1838-1913).  A block is an axis-aligned liquid region in
+ * normalized tank space [0,1]^3 (y up). */
+typedef struct fl_block {
+    float min[3];
+    float max[3];
+} fl_block;
+enum { FL_PRESET_FALLING_BLOB = 0, FL_PRESET_DAM_BREAK = 1, FL_PRESET_DOUBLE_SPLASH = 2 };
+#define FL_SCENE_MAX_BLOCKS 16u
+/* preset_blocks (scene/mod.rs:204-236): the preset's blocks for a drop height
+ * and a fill level in [0,1] (the registry's percentage / 100); `out` holds at
+ * least 2 blocks.  Unknown presets are the falling blob (ScenePreset::from_u32). */
+fl_status fl_scene_blocks(uint32_t preset, float drop_height, float fill_level, fl_block* out, uint32_t* n_out);
+/* seeded_volume_fraction (scene/mod.rs:155-165). */
+fl_status fl_scene_seeded_fraction(const fl_block* blocks, uint32_t nblocks, float* out);
+/* resolved_particle_count (scene/mod.rs:178-192): override_count when nonzero,
+ * else round(seeded cells * density), at least 1024 (0 for an empty scene). */
+fl_status fl_scene_particle_count(uint32_t nx, uint32_t ny, uint32_t nz, const fl_block* blocks, uint32_t nblocks,
+                                  float density, uint32_t override_count, uint32_t* out);
+/* Number of particles generate_particles lays out for these blocks and budget
+ * in the settings' tank (origin, cell size h = geom[0], extent = gdim * h). */
+fl_status fl_seed_count(const fl_params* params, const fl_block* blocks, uint32_t nblocks, uint32_t particle_count,
+                        uint32_t* n_out);
+/* generate_particles on the device, into the handle (like fl_set_particles:
+ * ids 0..n-1, zero velocity, the state fl_reset restores, pressure zeroed):
+ * the jittered lattice per block with the reference's seeded LCG, bit for bit.
+ * *n_out = particles written; INVALID_ARG if more than the capacity. */
+fl_status fl_seed_particles(fl_handle* h, const fl_block* blocks, uint32_t nblocks, uint32_t particle_count,
+                            uint32_t* n_out);
+
+/* ---- headless grid slice ----
+ * The per-cell arithmetic of the reference's slice debug renderer
+ * (app/crates/fluid-lab/src/gpu/slice.rs, shaders/slice.wgsl:69-141) for the
+ * XY cross-section at k (FL_SLICE_MIDDLE = nz/2, the reference's slice): one
+ * float4 {r, g, b, visible} per cell, row-major over (i, j), of the last
+ * substep's grid.  visible = 0 where the renderer draws nothing (air in
+ * FL_SLICE_CELL_TYPE; non-liquid cells in the other modes).  No window,
+ * swapchain or graphics API: the image is a buffer.  fl_grid_slice copies
+ * nx*ny*4 floats to host memory and waits; fl_grid_slice_device writes a
+ * 16-byte aligned device buffer on the handle's stream. */
+#define FL_SLICE_MIDDLE 0xffffffffu
+enum { FL_SLICE_CELL_TYPE = 0, FL_SLICE_PRESSURE = 1, FL_SLICE_SPEED = 2 };
+fl_status fl_grid_slice(fl_handle* h, uint32_t mode, uint32_t slice_k, float* rgba_out);
+fl_status fl_grid_slice_device(fl_handle* h, uint32_t mode, uint32_t slice_k, void* rgba_dev);
+
+/* ---- fixed-timestep frame driver ----
+ * fl_timestep restates the reference's TimestepController
+ * (app/crates/fluid-lab/src/timestep.rs:64-233): a render delta is sanitised,
+ * scaled by the simulation speed and clamped to 1/30 s before it enters the
+ * accumulator; at most max_substeps substeps of fixed_dt run per frame, and
+ * when more were due the rest of the accumulator is dropped.  Host only; no
+ * device is needed. */
+enum { FL_POLICY_FIXED_DROP_CAP = 0, FL_POLICY_EXPLICIT_EXPORT = 1 };
+typedef struct fl_timestep_stats {  /* TimestepFrameStats (timestep.rs:21-50) */
+    uint32_t substeps;          /* substeps executed this frame */
+    uint32_t natural_substeps;  /* substeps the accumulator wanted before the cap */
+    uint32_t max_substeps;
+    uint32_t substep_cap_hit;   /* 1 when natural_substeps > max_substeps */
+    float fixed_dt;
+    float accumulated_before;   /* accumulator after adding the clamped delta */
+    float accumulated_after;    /* after draining (and dropping) */
+    float dropped_this_frame;   /* seconds dropped by the cap this frame */
+    float sim_advanced;         /* seconds of simulation advanced */
+    float wall_dt;              /* sanitised render delta, before the clamp */
+    float sim_time_scale;
+    float real_time_factor;     /* sim_advanced / wall_dt (0 when wall_dt is 0) */
+    uint32_t policy;            /* FL_POLICY_* (label: fl_timestep_policy_label) */
+} fl_timestep_stats;
+typedef struct fl_timestep fl_timestep;
+fl_status fl_timestep_create(float fixed_dt, uint32_t max_substeps, fl_timestep** out);
+fl_status fl_timestep_free(fl_timestep* t);
+/* steps_for_frame_scaled (timestep.rs:98-150); sim_time_scale 1 = steps_for_frame. */
+fl_status fl_timestep_steps_for_frame(fl_timestep* t, float render_dt_s, float sim_time_scale, uint32_t* n_out);
+fl_status fl_timestep_record_manual_steps(fl_timestep* t, float render_dt_s, uint32_t substeps,
+                                          float sim_time_scale);
+fl_status fl_timestep_record_export_steps(fl_timestep* t, float sim_dt_s, uint32_t substeps);
+fl_status fl_timestep_record_idle_frame(fl_timestep* t, float render_dt_s, float sim_time_scale);
+fl_status fl_timestep_reset(fl_timestep* t);
+fl_status fl_timestep_last_stats(const fl_timestep* t, fl_timestep_stats* out);
+fl_status fl_timestep_total_dropped(const fl_timestep* t, float* out);
+fl_status fl_timestep_accumulator(const fl_timestep* t, float* out);
+const char* fl_timestep_policy_label(uint32_t policy);
+/* The simulation half of FluidApp::frame (app/crates/fluid-lab/src/lib.rs:352-394):
+ * running, accumulate render_dt_ms (sanitised, converted to seconds in f32)
+ * scaled by sim_speed and run the due substeps on h; paused, reset the
+ * accumulator and run one substep if *pending_steps > 0 (decrementing it).
+ * *substeps_out (may be NULL) receives the substeps run. */
+fl_status fl_frame(fl_handle* h, fl_timestep* t, double render_dt_ms, float sim_speed, int paused,
+                   uint32_t* pending_steps, uint32_t* substeps_out);
+/* The simulation half of FluidApp::export_frame (lib.rs:570-590): run
+ * `substeps` substeps and record them as explicit export steps. */
+fl_status fl_export_frame(fl_handle* h, fl_timestep* t, uint32_t substeps, double sim_dt_s);
 
 /* Stand-alone pressure solve on host arrays: the MAC-Poisson CG of
  * cg_init/cg_spmv/.../cg_dir.wgsl with the step's semantics, for cell types

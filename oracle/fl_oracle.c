@@ -469,3 +469,133 @@ float orc_ref_max_abs_divergence(uint32_t n_cells, const float* div, const uint8
         if (ct[c] == FL_CELL_LIQUID) m = fmaxf(m, fabsf(div[c]));
     return m;
 }
+
+/* ---- slice.wgsl:41-141: WGSL mix(e1, e2, e3) = e1*(1-e3) + e2*e3, clamp =
+ * min(max(e, lo), hi), length = sqrt(x*x + y*y + z*z); all in f32. */
+static float slice_mix(float a, float b, float s) { return a * (1.0f - s) + b * s; }
+static float slice_clamp01(float t) { return fminf(fmaxf(t, 0.0f), 1.0f); }
+static void slice_mix3(const float a[3], const float b[3], float s, float out[3]) {
+    for (int c = 0; c < 3; c++) out[c] = slice_mix(a[c], b[c], s);
+}
+static void slice_diverging(float t, float out[3]) {
+    static const float blue[3] = {0.0f, 0.2f, 0.9f}, white[3] = {1.0f, 1.0f, 1.0f}, red[3] = {0.9f, 0.05f, 0.05f};
+    const float tc = slice_clamp01(t);
+    if (tc < 0.5f) slice_mix3(blue, white, tc * 2.0f, out);
+    else slice_mix3(white, red, (tc - 0.5f) * 2.0f, out);
+}
+static void slice_speed(float t, float out[3]) {
+    static const float c0[3] = {0.0f, 0.0f, 0.8f}, c1[3] = {0.0f, 0.9f, 0.9f}, c2[3] = {1.0f, 1.0f, 0.0f},
+                       c3[3] = {0.9f, 0.0f, 0.0f};
+    const float tc = slice_clamp01(t);
+    if (tc < 0.333f) slice_mix3(c0, c1, tc / 0.333f, out);
+    else if (tc < 0.667f) slice_mix3(c1, c2, (tc - 0.333f) / 0.333f, out);
+    else slice_mix3(c2, c3, (tc - 0.667f) / 0.333f, out);
+}
+
+void orc_grid_slice(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* ct, const float* p, const float* u,
+                    const float* v, const float* w, uint32_t mode, uint32_t k, float* rgba_out) {
+    (void)nz;
+    for (uint32_t j = 0; j < ny; j++)
+        for (uint32_t i = 0; i < nx; i++) {
+            const size_t idx = (size_t)i + nx * ((size_t)j + (size_t)ny * k);
+            const uint8_t t = ct[idx];
+            float c[3] = {0.0f, 0.0f, 0.0f};
+            int visible;
+            if (mode == 0u) {
+                visible = t != FL_CELL_AIR;
+                if (t == FL_CELL_SOLID) { c[0] = 0.40f; c[1] = 0.40f; c[2] = 0.46f; }
+                else { c[0] = 0.20f; c[1] = 0.55f; c[2] = 1.00f; }
+            } else if (mode == 1u) {
+                visible = t == FL_CELL_LIQUID;
+                if (visible) slice_diverging(slice_clamp01(p[idx] / 2000.0f * 0.5f + 0.5f), c);
+            } else {
+                visible = t == FL_CELL_LIQUID;
+                if (visible) {
+                    const float u0 = u[i + (size_t)(nx + 1) * (j + (size_t)ny * k)];
+                    const float u1 = u[(i + 1) + (size_t)(nx + 1) * (j + (size_t)ny * k)];
+                    const float v0 = v[i + (size_t)nx * (j + (size_t)(ny + 1) * k)];
+                    const float v1 = v[i + (size_t)nx * ((j + 1) + (size_t)(ny + 1) * k)];
+                    const float w0 = w[i + (size_t)nx * (j + (size_t)ny * k)];
+                    const float w1 = w[i + (size_t)nx * (j + (size_t)ny * (k + 1))];
+                    const float au = (u0 + u1) * 0.5f, av = (v0 + v1) * 0.5f, aw = (w0 + w1) * 0.5f;
+                    const float spd = sqrtf(au * au + av * av + aw * aw);
+                    slice_speed(slice_clamp01(spd / 4.0f), c);
+                }
+            }
+            float* o = rgba_out + 4 * ((size_t)i + (size_t)nx * j);
+            o[0] = c[0]; o[1] = c[1]; o[2] = c[2]; o[3] = visible ? 1.0f : 0.0f;
+        }
+}
+
+/* ---- gpu/fluid.rs:1838-1913 generate_particles, sequential (f32) ---- */
+static float rust_clampf(float x, float lo, float hi) {
+    if (x < lo) x = lo;
+    if (x > hi) x = hi;
+    return x;
+}
+static int32_t rust_f32_to_i32(float q) {
+    if (q != q) return 0;
+    if (q >= 2147483647.0f) return 2147483647;
+    if (q <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)q;
+}
+
+uint32_t orc_ref_generate_particles(const float origin[3], float h, const uint32_t gdim[3], const float* blocks,
+                                    uint32_t nblocks, uint32_t particle_count, float* out, uint32_t capacity) {
+    float extent[3], lo[3], hi[3];
+    for (int a = 0; a < 3; a++) {
+        extent[a] = (float)gdim[a] * h;
+        lo[a] = origin[a] + h * 1.05f;
+        hi[a] = origin[a] + extent[a] - h * 1.05f;
+    }
+    float total_vol = 0.0f;
+    for (uint32_t b = 0; b < nblocks; b++) {
+        float e[3];
+        for (int a = 0; a < 3; a++) {
+            const float wmin = origin[a] + blocks[6 * b + a] * extent[a];
+            const float wmax = origin[a] + blocks[6 * b + 3 + a] * extent[a];
+            e[a] = wmax - wmin;
+        }
+        total_vol += fmaxf(e[0] * e[1] * e[2], 1e-6f);
+    }
+    total_vol = fmaxf(total_vol, 1e-6f);
+    const float total_target = (float)(particle_count > 1u ? particle_count : 1u);
+    uint32_t st = 0x12345678u;
+    uint32_t n = 0;
+    for (uint32_t b = 0; b < nblocks; b++) {
+        float wmin[3], e[3];
+        for (int a = 0; a < 3; a++) {
+            wmin[a] = origin[a] + blocks[6 * b + a] * extent[a];
+            const float wmax = origin[a] + blocks[6 * b + 3 + a] * extent[a];
+            e[a] = wmax - wmin[a];
+        }
+        const float vol = fmaxf(e[0] * e[1] * e[2], 1e-6f);
+        const float target = fmaxf(total_target * (vol / total_vol), 1.0f);
+        const float spacing = fmaxf(cbrtf(vol / target), 1e-4f);
+        int32_t cnt[3];
+        for (int a = 0; a < 3; a++) {
+            const int32_t c = rust_f32_to_i32(floorf(e[a] / spacing));
+            cnt[a] = c > 1 ? c : 1;
+        }
+        for (int32_t ix = 0; ix < cnt[0]; ix++)
+            for (int32_t iy = 0; iy < cnt[1]; iy++)
+                for (int32_t iz = 0; iz < cnt[2]; iz++) {
+                    const int32_t idx[3] = {ix, iy, iz};
+                    float pos[3];
+                    for (int a = 0; a < 3; a++) {
+                        st = st * 1664525u + 1013904223u;
+                        const float r = (float)(st >> 8) / 16777216.0f;
+                        const float j = (r - 0.5f) * spacing * 0.5f;
+                        pos[a] = rust_clampf(wmin[a] + ((float)idx[a] + 0.5f) * spacing + j, lo[a], hi[a]);
+                    }
+                    if (n < capacity) {
+                        float* o = out + 8 * (size_t)n;
+                        o[0] = pos[0]; o[1] = pos[1]; o[2] = pos[2];
+                        o[3] = o[4] = o[5] = o[6] = o[7] = 0.0f;
+                    }
+                    n++;
+                }
+    }
+    return n;
+}
+

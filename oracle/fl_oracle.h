@@ -107,6 +107,19 @@ void orc_ref_subtract_gradient(uint32_t nx, uint32_t ny, uint32_t nz, float h, f
 float orc_ref_l2_divergence(uint32_t n_cells, const float* div, const uint8_t* ct);
 float orc_ref_max_abs_divergence(uint32_t n_cells, const float* div, const uint8_t* ct);
 
+/* generate_particles (gpu/fluid.rs:1838-1913) as the reference runs it: one
+ * sequential loop over blocks and lattice points drawing from a single seeded
+ * LCG.  blocks: 6 floats each (min xyz, max xyz, normalized).  Writes up to
+ * `capacity` particles (8 floats each, zero velocity); returns the layout's
+ * particle count. */
+uint32_t orc_ref_generate_particles(const float origin[3], float h, const uint32_t gdim[3], const float* blocks,
+                                    uint32_t nblocks, uint32_t particle_count, float* out, uint32_t capacity);
+
+/* The per-cell arithmetic of the slice debug renderer (shaders/slice.wgsl:69-141)
+ * for the XY slice at k: rgba_out[4*(i + nx*j) + c] = {r, g, b, visible}. */
+void orc_grid_slice(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* ct, const float* p, const float* u,
+                    const float* v, const float* w, uint32_t mode, uint32_t k, float* rgba_out);
+
 #ifdef __cplusplus
 }
 #endif

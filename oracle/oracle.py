@@ -96,6 +96,10 @@ def load(build=True):
     lib.orc_ref_l2_divergence.argtypes = [_u32, _fp, _u8p_t]
     lib.orc_ref_max_abs_divergence.restype = ctypes.c_float
     lib.orc_ref_max_abs_divergence.argtypes = [_u32, _fp, _u8p_t]
+    lib.orc_ref_generate_particles.restype = _u32
+    lib.orc_ref_generate_particles.argtypes = [_fp, ctypes.c_float, _u32p_t, _fp, _u32, _u32, _fp, _u32]
+    lib.orc_grid_slice.restype = None
+    lib.orc_grid_slice.argtypes = [_u32, _u32, _u32, _u8p_t, _fp, _fp, _fp, _fp, _u32, _u32, _fp]
     _lib = lib
     return lib
 
@@ -367,3 +371,28 @@ def ref_max_abs_divergence(div, ct):
     lib = load()
     return float(lib.orc_ref_max_abs_divergence(div.size, f32p(np.ascontiguousarray(div, np.float32)),
                                                 u8p(np.ascontiguousarray(ct, np.uint8))))
+
+
+def grid_slice(dims, ct, p, u, v, w, mode, k=None):
+    """The slice renderer's per-cell colours (orc_grid_slice): (ny, nx, 4) float32."""
+    lib = load()
+    nx, ny, nz = dims
+    k = nz // 2 if k is None else k
+    out = np.empty((ny, nx, 4), np.float32)
+    arrs = [np.ascontiguousarray(a, np.float32) for a in (p, u, v, w)]
+    ctc = np.ascontiguousarray(ct, np.uint8)
+    lib.orc_grid_slice(nx, ny, nz, u8p(ctc), *[f32p(a) for a in arrs], mode, k, f32p(out))
+    return out
+
+
+def ref_generate_particles(params, blocks, particle_count, capacity):
+    """generate_particles (fluid.rs:1838-1913), sequential: (n, particles[:n])."""
+    lib = load()
+    origin = np.array(params.origin[:3], np.float32)
+    gdim = np.array(params.gdim[:3], np.uint32)
+    b = np.array([[*blk.min, *blk.max] for blk in blocks], np.float32).reshape(-1)
+    out = np.zeros((capacity, 8), np.float32)
+    n = lib.orc_ref_generate_particles(f32p(origin), params.geom[0], u32p(gdim), f32p(b), len(blocks),
+                                       particle_count, f32p(out), capacity)
+    return n, out[:min(n, capacity)]
+

@@ -14,15 +14,16 @@
 //   k_adj_g2p       g2p.wgsl:131-198 (forward Euler, friction off): particle
 //                   gradients w.r.t. position and velocity, and face gradients
 //                   of the final and saved velocities (scatter = transpose of
-//                   the trilinear gather; float atomics)
+//                   the trilinear gather; one float2 vector atomic per tap into
+//                   the interleaved {final, saved} gradients)
 //   k_adj_prhs      gradient.wgsl transposed: dL/dp per liquid cell, the RHS
 //                   of the adjoint pressure solve A lambda = dL/dp
 //   (k_solve_init + k_cg with the RHS: the adjoint solve)
 //   k_adj_faces     divergence.wgsl and gradient.wgsl transposed, then
 //                   boundaries.wgsl / forces.wgsl / save_vel.wgsl: gradient of
 //                   the normalised P2G face velocity, and dL/dgravity
-//   k_adj_p2g_sums  scatter.wgsl without the fixed-point rounding (float
-//                   atomics): sum w and sum w v per face
+//   k_adj_p2g_sums  scatter.wgsl without the fixed-point rounding: {sum w,
+//                   sum w v} per face (one float2 vector atomic per tap)
 //   k_adj_p2g       scatter.wgsl transposed: a gather from faces to particles
 //                   (velocity and position gradients)
 //   k_adj_unsort    sort_scatter.wgsl transposed: back to the step's input order
@@ -86,7 +87,7 @@ __global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
         const float X[3] = {pos.x, pos.y, pos.z}, pv[3] = {pvel.x, pvel.y, pvel.z};
         const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
         // forward recompute: pic, saved, their position derivatives
-        float pic[3], sv[3], dpic[3][3], dsv[3][3];
+        float pic[3], sv[3], dpic[3][3], dsv[3][3], W[3];
         for (int ax = 0; ax < 3; ax++) {
             float fsum = 0.0f, ssum = 0.0f, wsum = 0.0f, dws[3] = {0, 0, 0}, dfs[3] = {0, 0, 0}, dss[3] = {0, 0, 0};
             const float* fv = a.fin[ax];
@@ -102,6 +103,7 @@ __global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
                     dss[b] += dw[b] * s;
                 }
             });
+            W[ax] = wsum;
             if (wsum > 0.0f) {
                 pic[ax] = fsum / wsum;
                 sv[ax] = ssum / wsum;
@@ -152,17 +154,14 @@ __global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
         }
         for (int b = 0; b < 3; b++)
             for (int ax = 0; ax < 3; ax++) gX[b] += gpic[ax] * dpic[ax][b] + gsv[ax] * dsv[ax][b];
-        // face gradients: pic_ax = sum (w/W) fin_f
+        // face gradients: pic_ax = sum (w/W) fin_f, saved likewise
         for (int ax = 0; ax < 3; ax++) {
-            float wsum = 0.0f;
-            stencil(P, ax, q, true, [&](size_t, float w, const float*) { wsum += w; });
-            if (!(wsum > 0.0f)) continue;
-            const float cf = gpic[ax] / wsum, cs = gsv[ax] / wsum;
-            float* gf = a.g_fin[ax];
-            float* gs = a.g_sav[ax];
+            if (!(W[ax] > 0.0f)) continue;
+            const float cf = gpic[ax] / W[ax], cs = gsv[ax] / W[ax];
+            if (cf == 0.0f && cs == 0.0f) continue;
+            float2* gfs = a.g_fs[ax];
             stencil(P, ax, q, true, [&](size_t idx, float w, const float*) {
-                if (cf != 0.0f) atomicAdd(&gf[idx], w * cf);
-                if (cs != 0.0f) atomicAdd(&gs[idx], w * cs);
+                atomicAdd(gfs + idx, make_float2(w * cf, w * cs));
             });
         }
         a.g_sorted[2 * (size_t)d] = make_float4(gX[0], gX[1], gX[2], 0.0f);
@@ -195,7 +194,7 @@ __global__ void __launch_bounds__(256) k_adj_prhs(AdjBufs a) {
                 const size_t fidx = (size_t)f3[0] + dx * ((size_t)f3[1] + (size_t)dy * f3[2]);
                 const size_t other = side == 0 ? c - step[ax] : c + step[ax];
                 if (!grad_face(a.ct[side == 0 ? other : c], a.ct[side == 0 ? c : other])) continue;
-                const float g = a.g_fin[ax][fidx];
+                const float g = a.g_fs[ax][fidx].x;
                 acc += side == 0 ? g : -g;
             }
         }
@@ -224,7 +223,8 @@ __global__ void __launch_bounds__(256) k_adj_faces(AdjBufs a, int axis) {
         float gpre = 0.0f;
         if (!solid) {
             // vel_final = vel_pre - coeff*(p_hi - p_lo) on gradient faces; p = A^-1(-scale*div(vel_pre))
-            float g = a.g_fin[axis][f];
+            const float2 gfs = a.g_fs[axis][f];
+            float g = gfs.x;
             float dl = 0.0f;
             if (tl == CELL_LIQUID) dl += a.lam[hi_c - step];
             if (th == CELL_LIQUID) dl -= a.lam[hi_c];
@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(256) k_adj_faces(AdjBufs a, int axis) {
             const bool wet = tl == CELL_LIQUID || th == CELL_LIQUID;
             if (wet) gg = (double)gpre * (double)P.dt;
         }
-        a.g_norm[axis][f] = gpre + a.g_sav[axis][f];
+        a.g_norm[axis][f] = gpre + a.g_fs[axis][f].y;
     }
     // dL/dg_axis (fixed order within the block, atomics across blocks)
 #pragma unroll
@@ -260,11 +260,9 @@ __global__ void __launch_bounds__(256) k_adj_p2g_sums(AdjBufs a) {
         const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
         const float pv[3] = {pvel.x, pvel.y, pvel.z};
         for (int ax = 0; ax < 3; ax++) {
-            float* ws = a.w_sum[ax];
-            float* wvs = a.wv_sum[ax];
+            float2* ws = a.wsum[ax];
             stencil(P, ax, q, false, [&](size_t idx, float w, const float*) {
-                atomicAdd(ws + idx, w);
-                atomicAdd(wvs + idx, w * pv[ax]);
+                atomicAdd(ws + idx, make_float2(w, w * pv[ax]));
             });
         }
     }
@@ -280,15 +278,15 @@ __global__ void __launch_bounds__(256) k_adj_p2g(AdjBufs a) {
         const float pv[3] = {pvel.x, pvel.y, pvel.z};
         float gX[3] = {0, 0, 0}, gv[3] = {0, 0, 0};
         for (int ax = 0; ax < 3; ax++) {
-            const float* ws = a.w_sum[ax];
-            const float* wvs = a.wv_sum[ax];
+            const float2* ws = a.wsum[ax];
             const float* gn = a.g_norm[ax];
             stencil(P, ax, q, false, [&](size_t idx, float w, const float* dw) {
-                const float W = ws[idx];
+                const float2 s = ws[idx];
+                const float W = s.x;
                 if (!(W > 0.0f)) return;
                 const float g = gn[idx] / W;
                 gv[ax] += w * g;
-                const float diff = (pv[ax] - wvs[idx] / W) * g * inv_h;
+                const float diff = (pv[ax] - s.y / W) * g * inv_h;
                 for (int b = 0; b < 3; b++) gX[b] += dw[b] * diff;
             });
         }

@@ -117,13 +117,11 @@ struct AdjBufs {
     const float4* g_out;     // dL/d(output particle d), bin order, 2 float4 each
     float4* g_sorted;        // dL/d(input particle in bin order), 2 float4 each
     float4* g_in;            // dL/d(input particle), input order
-    float* g_fin[3];
-    float* g_sav[3];
+    float2* g_fs[3];         // {dL/d final face velocity, dL/d saved face velocity} per face
     float* g_norm[3];
-    // Unquantised P2G sums sum w and sum w v of the recorded step (scratch that
-    // aliases g_fin / g_sav once k_adj_faces has consumed those).
-    float* w_sum[3];
-    float* wv_sum[3];
+    // Unquantised P2G sums {sum w, sum w v} of the recorded step (scratch that
+    // aliases g_fs once k_adj_faces has consumed it).
+    float2* wsum[3];
     float* lam;              // adjoint pressure (the solve's x)
     float* rhs;              // dL/dp
     double* g_grav;          // 3 accumulators

@@ -937,8 +937,7 @@ struct fl_tape {
     char* slots = nullptr;
     size_t slot_bytes = 0, o_part = 0, o_perm = 0, o_ct = 0, o_sav[3] = {}, o_fin[3] = {};
     float4* g_sorted = nullptr;
-    float* g_fin[3] = {};
-    float* g_sav[3] = {};
+    float2* g_fs[3] = {};
     float* g_norm[3] = {};
     float* rhs = nullptr;
     double* g_grav = nullptr;
@@ -969,10 +968,9 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     t->slot_bytes = (slot.off + 255) & ~size_t(255);
     PoolPlan pl;
     pl.off = t->slot_bytes * max_steps;
-    size_t o_gs = pl.take<float4>(2 * cap), o_gf[3], o_gv[3], o_gn[3];
+    size_t o_gs = pl.take<float4>(2 * cap), o_gf[3], o_gn[3];
     for (int a = 0; a < 3; a++) {
-        o_gf[a] = pl.take<float>(h->F3[a]);
-        o_gv[a] = pl.take<float>(h->F3[a]);
+        o_gf[a] = pl.take<float2>(h->F3[a]);
         o_gn[a] = pl.take<float>(h->F3[a]);
     }
     size_t o_rhs = pl.take<float>(C), o_lam = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C),
@@ -992,8 +990,7 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     t->slots = base;
     t->g_sorted = (float4*)(base + o_gs);
     for (int a = 0; a < 3; a++) {
-        t->g_fin[a] = (float*)(base + o_gf[a]);
-        t->g_sav[a] = (float*)(base + o_gv[a]);
+        t->g_fs[a] = (float2*)(base + o_gf[a]);
         t->g_norm[a] = (float*)(base + o_gn[a]);
     }
     t->rhs = (float*)(base + o_rhs);
@@ -1091,13 +1088,10 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     for (int ax = 0; ax < 3; ax++) {
         a.sav[ax] = (const float*)(slot + t->o_sav[ax]);
         a.fin[ax] = (const float*)(slot + t->o_fin[ax]);
-        a.g_fin[ax] = t->g_fin[ax];
-        a.g_sav[ax] = t->g_sav[ax];
+        a.g_fs[ax] = t->g_fs[ax];
         a.g_norm[ax] = t->g_norm[ax];
-        a.w_sum[ax] = t->g_fin[ax];   // free once k_adj_faces has run
-        a.wv_sum[ax] = t->g_sav[ax];
-        FL_CUDA(h, cudaMemsetAsync(t->g_fin[ax], 0, 4 * (size_t)h->F3[ax], st));
-        FL_CUDA(h, cudaMemsetAsync(t->g_sav[ax], 0, 4 * (size_t)h->F3[ax], st));
+        a.wsum[ax] = t->g_fs[ax];  // free once k_adj_faces has run
+        FL_CUDA(h, cudaMemsetAsync(t->g_fs[ax], 0, sizeof(float2) * (size_t)h->F3[ax], st));
     }
     a.g_out = (const float4*)dL_dout_dev;
     a.g_sorted = t->g_sorted;
@@ -1129,8 +1123,7 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
     FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));
     for (int ax = 0; ax < 3; ax++) {
-        FL_CUDA(h, cudaMemsetAsync(a.w_sum[ax], 0, 4 * (size_t)h->F3[ax], st));
-        FL_CUDA(h, cudaMemsetAsync(a.wv_sum[ax], 0, 4 * (size_t)h->F3[ax], st));
+        FL_CUDA(h, cudaMemsetAsync(a.wsum[ax], 0, sizeof(float2) * (size_t)h->F3[ax], st));
     }
     FL_CUDA(h, fl::launch_adj_p2g_sums(a, h->L, st));
     FL_CUDA(h, fl::launch_adj_p2g(a, h->L, st));

@@ -51,6 +51,10 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--adj-steps", type=int, default=20, help="rollout length of the forward+adjoint leg (0 = off)")
     ap.add_argument("--adj-every", type=int, default=10, help="checkpoint interval of that rollout")
+    ap.add_argument("--adj-no-plog", action="store_true",
+                    help="recompute segments with their pressure solves (default: replay the logged pressure fields)")
+    ap.add_argument("--adj-cold", action="store_true",
+                    help="start every adjoint pressure solve from zero (default: from the next step's solution)")
     return ap.parse_args()
 
 
@@ -202,19 +206,23 @@ def timed_steps(torch, g, k):
     return e0.elapsed_time(e1)
 
 
-def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol):
+def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol, warm=True, plog=True):
     """Forward+adjoint of a checkpointed rollout against its forward alone.
 
     forward: `steps` substeps from `parts` with a device checkpoint every
-    `every`, the last segment recorded on the tape; backward: per earlier
-    segment, restore + recompute while recording; every step popped through
+    `every`, the last segment recorded on the tape, and (with `plog`) every
+    substep's pressure field; backward: per earlier segment, restore +
+    recompute while recording (with `plog`, each substep replayed with its
+    logged pressure instead of its CG: the same bits); every step popped through
     the adjoint (second CG with the forward's iteration cap, tolerance and
-    precision).  Loss: |centre of mass - (0.7, 0.2, 0.5)|^2.  Timed with CUDA
+    precision, started from the next step's adjoint pressure unless `warm` is
+    False).  Loss: |centre of mass - (0.7, 0.2, 0.5)|^2.  Timed with CUDA
     events on the rollout's stream."""
     from fluidgb.autograd import Rollout
     n = parts.shape[0]
     free0 = torch.cuda.mem_get_info()[0]
-    roll = Rollout(p, n, steps, checkpoint_every=every, adj_cg_iters=cg_iters, adj_cg_tol=cg_tol)
+    roll = Rollout(p, n, steps, checkpoint_every=every, adj_cg_iters=cg_iters, adj_cg_tol=cg_tol,
+                   adj_warm_start=warm, pressure_log=plog)
     parts_d = torch.from_numpy(parts).cuda()
     target = torch.tensor([0.7, 0.2, 0.5], dtype=torch.float64, device="cuda")
     grav = (p.grav[0], p.grav[1], p.grav[2])
@@ -246,9 +254,13 @@ def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol):
     return {"workload_steps": steps, "checkpoint_every": every,
             "fwd_ms_per_step": fwd_ms / steps, "fwd_adj_ms_per_step": (fwd_ms + bwd_ms) / steps,
             "ratio": (fwd_ms + bwd_ms) / fwd_ms,
-            "backward": "last segment taped during the forward; earlier segments restore + recompute-with-tape; adjoint per step",
+            "backward": "last segment taped during the forward; earlier segments restore + recompute-with-tape" +
+                        (" (substeps replayed with their logged pressure fields, no CG)" if plog else " (CG re-solved)") +
+                        "; adjoint per step",
+            "pressure_log_bytes": steps * int(p.gdim[0]) * int(p.gdim[1]) * int(p.gdim[2]) * 4 if plog else 0,
             "adj_cg_iters_mean": float(sum(iters)) / max(len(iters), 1), "adj_cg_iters_max": max(iters or [0]),
             "adj_cg_max_iters": cg_iters, "adj_cg_tol": cg_tol,
+            "adj_cg_start": "warm: previous step's lambda, stop at |r| <= tol |dL/dp|" if warm else "cold: zero",
             "device_bytes": used, "device_bytes_note": "handle + tape + checkpoints + torch buffers of the rollout"}
 
 
@@ -320,7 +332,8 @@ def run_ours(args):
 
     adj = None
     if args.adj_steps > 0:
-        adj = adjoint_leg(torch, p, parts, args.adj_steps, args.adj_every, spec["iters"], spec["tol"])
+        adj = adjoint_leg(torch, p, parts, args.adj_steps, args.adj_every, spec["iters"], spec["tol"],
+                          warm=not args.adj_cold, plog=not args.adj_no_plog)
         torch.cuda.set_stream(stream)
 
     # Per-stage device times (CUDA events between stages on the same stream).

@@ -18,6 +18,7 @@
 //                   the interleaved {final, saved} gradients)
 //   k_adj_prhs      gradient.wgsl transposed: dL/dp per liquid cell, the RHS
 //                   of the adjoint pressure solve A lambda = dL/dp
+//   k_adj_thr       (warm start only) the solve's absolute stopping threshold
 //   (k_solve_init + k_cg with the RHS: the adjoint solve)
 //   k_adj_faces     divergence.wgsl and gradient.wgsl transposed, then
 //                   boundaries.wgsl / forces.wgsl / save_vel.wgsl: gradient of
@@ -175,12 +176,14 @@ __device__ __forceinline__ bool grad_face(uint8_t lt, uint8_t ht) {
 }
 
 // dL/dp_c = -coeff * (sum over gradient faces whose hi cell is c of g - ... whose lo cell is c).
+// One block per 256-cell chunk; with rhs_part set it also writes the chunk's
+// float-float sum of rhs^2 (fixed order: warp shuffles, then warps in order).
 __global__ void __launch_bounds__(256) k_adj_prhs(AdjBufs a) {
+    __shared__ float2 s_red[8];
     const DevParams& P = *a.prm;
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= P.C) return;
     float acc = 0.0f;
-    if (a.ct[c] == CELL_LIQUID) {
+    if (c < P.C && a.ct[c] == CELL_LIQUID) {
         const uint32_t nx = P.nx, ny = P.ny;
         const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
         const uint32_t ijk[3] = {i, j, k};
@@ -200,7 +203,40 @@ __global__ void __launch_bounds__(256) k_adj_prhs(AdjBufs a) {
         }
         acc *= -P.coeff_grad;
     }
-    a.rhs[c] = acc;
+    if (c < P.C) a.rhs[c] = acc;
+    if (a.rhs_part) {
+        const Df sq = warp_sum_df(df_prod(acc, acc));
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = make_float2(sq.hi, sq.lo);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            Df t = {0.0f, 0.0f};
+            for (int w = 0; w < 8; w++) t = df_add(t, Df{s_red[w].x, s_red[w].y});
+            a.rhs_part[blockIdx.x] = make_float2(t.hi, t.lo);
+        }
+    }
+}
+
+// Absolute stopping threshold of the warm-started adjoint solve: tol^2 times
+// the squared norm of its right-hand side, the value the cold-start test
+// tol^2 * (r0.r0) uses (r0 = rhs when the solve starts from zero).  One block;
+// the chunk partials are summed in a fixed order.
+__global__ void __launch_bounds__(1024) k_adj_thr(const float2* __restrict__ part, uint32_t nchunks, double tol_sq,
+                                                  DevParams* __restrict__ cg_prm) {
+    __shared__ float2 s_red[32];
+    Df t = {0.0f, 0.0f};
+    for (uint32_t i = threadIdx.x; i < nchunks; i += blockDim.x) t = df_add(t, Df{part[i].x, part[i].y});
+    t = warp_sum_df(t);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    if (lane == 0) s_red[warp] = make_float2(t.hi, t.lo);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Df s = {0.0f, 0.0f};
+        for (uint32_t w = 0; w < blockDim.x / 32; w++) s = df_add(s, Df{s_red[w].x, s_red[w].y});
+        const double thr = tol_sq * ((double)s.hi + (double)s.lo);
+        cg_prm->thr_abs_d = thr;
+        cg_prm->thr_abs_f = (float)thr;
+        cg_prm->thr_abs = 1u;
+    }
 }
 
 // Face stage: projection (divergence transposed), boundaries, forces, save_vel.
@@ -313,6 +349,10 @@ cudaError_t launch_adj_g2p(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s)
 }
 cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s) {
     k_adj_prhs<<<(C + 255) / 256, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_thr(const AdjBufs& a, uint32_t nchunks, double tol_sq, DevParams* cg_prm, cudaStream_t s) {
+    k_adj_thr<<<1, 1024, 0, s>>>(a.rhs_part, nchunks, tol_sq, cg_prm);
     return cudaGetLastError();
 }
 cudaError_t launch_adj_faces(const AdjBufs& a, const uint32_t F3[3], cudaStream_t s) {

@@ -67,6 +67,7 @@ struct CgShared {
     float red[2 * CG_WARPS];   // float-float warp partials
     uint32_t wcnt[CG_WARPS];
     uint32_t layout, nslot;              // exchange slot layout (0 plan order, 1 lines, 2 one line per block), slots used
+    float thr_f;                         // f32 stopping threshold on r.r
     uint32_t bstart[MAX_CG_BLOCKS + 1];  // first plan entry of every block
     uint32_t spos[MAX_CG_BLOCKS + 1];    // first exchange slot of every block
     uint16_t lineblk[VAL_CAP / 16 + MAX_CG_BLOCKS];  // line of the slot area -> owning block
@@ -538,8 +539,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         }
         __syncthreads();
         rs_old_d = rs_init_d = warp_allsum_df(Df{sh.red[2 * lane], sh.red[2 * lane + 1]});
-        // stopping threshold tol^2 * rs_init, once per solve
-        const double thr = tol_sq_d * df_to_double(rs_init_d);
+        // stopping threshold tol^2 * rs_init (or the absolute one), once per solve
+        const double thr = P.thr_abs ? P.thr_abs_d : tol_sq_d * df_to_double(rs_init_d);
         thr_d.hi = (float)thr;
         thr_d.lo = (float)(thr - (double)thr_d.hi);
         __syncthreads();  // sh.red is reused
@@ -547,6 +548,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         reduce_f32(nullptr, 0u, false, rs_old_f);
         rs_init_f = rs_old_f;
     }
+    // Thresholds and rs_init are stored once here, not held in registers
+    // through the loop.  f32: tol^2 * rs_init (cg_beta.wgsl:25-30) or the
+    // absolute threshold.
+    if (tid == 0) {
+        if (!f64) sh.thr_f = P.thr_abs ? P.thr_abs_f : __fmul_rn(tol_sq, rs_init_f);
+        if (blockIdx.x == 0) st->rs_init = f64 ? df_to_double(rs_init_d) : (double)rs_init_f;
+    }
+    __syncthreads();
 
     float beta = 0.0f;
     uint32_t k = 0, tag = tag_base;
@@ -739,13 +748,12 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             if (!reduce_f32(slotB, tag, true, rs_new)) return;
             beta = rs_old_f > 1e-30f ? __fdiv_rn(rs_new, rs_old_f) : 0.0f;  // cg_beta.wgsl:16-23
             rs_old_f = rs_new;
-            done = stop_on && rs_new <= __fmul_rn(tol_sq, rs_init_f);  // cg_beta.wgsl:25-30
+            done = stop_on && rs_new <= sh.thr_f;
         }
         if (done) break;
     }
     if (blockIdx.x == 0 && tid == 0) {
         st->cg_iters = k;
-        st->rs_init = f64 ? df_to_double(rs_init_d) : (double)rs_init_f;
         st->rs_final = f64 ? df_to_double(rs_old_d) : (double)rs_old_f;
     }
 }

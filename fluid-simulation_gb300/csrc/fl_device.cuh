@@ -38,6 +38,12 @@ struct DevParams {
     uint32_t thresh, dilation, warm, iters;
     uint32_t precision, advect_order, nchunks, pad1;
     double tol_sq_d;
+    // Absolute stopping threshold on r.r, used instead of tol^2 * (r0.r0) when
+    // thr_abs is 1 (the warm-started adjoint solve: tol^2 * |rhs|^2, written
+    // on the device by k_adj_thr before the solve).
+    double thr_abs_d;
+    float thr_abs_f;
+    uint32_t thr_abs;
 };
 
 // Per-step device counters and results.
@@ -124,6 +130,7 @@ struct AdjBufs {
     float2* wsum[3];
     float* lam;              // adjoint pressure (the solve's x)
     float* rhs;              // dL/dp
+    float2* rhs_part;        // per-chunk float-float partials of rhs.rhs (null: not needed)
     double* g_grav;          // 3 accumulators
 };
 
@@ -277,6 +284,8 @@ cudaError_t launch_seed(const SeedArgs& a, float4* part, cudaStream_t s);
 struct AdjBufs;
 cudaError_t launch_adj_g2p(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s);
+// tol^2 * (rhs.rhs) into cg_prm's absolute threshold (rhs_part of a block-per-chunk k_adj_prhs)
+cudaError_t launch_adj_thr(const AdjBufs& a, uint32_t nchunks, double tol_sq, DevParams* cg_prm, cudaStream_t s);
 cudaError_t launch_adj_faces(const AdjBufs& a, const uint32_t F3[3], cudaStream_t s);
 cudaError_t launch_adj_p2g_sums(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_adj_p2g(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);

@@ -175,8 +175,11 @@ fl::LaunchCfg make_cfg(uint32_t nchunks) {
 }
 
 // Enqueue one substep.  The caller set b.part_in/out/ids.  With `ev`, an
-// event is recorded before the first stage and after every stage.
-cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEvent_t* ev = nullptr) {
+// event is recorded before the first stage and after every stage.  With
+// `p_replay`, the pressure solve is replaced by a copy of that pressure field
+// (C floats): the substep that produced it is reproduced without its CG.
+cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEvent_t* ev = nullptr,
+                         const float* p_replay = nullptr) {
     cudaError_t e;
     auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
     if ((e = cudaMemsetAsync(h->dst, 0, fl::DEVSTATS_STEP_BYTES, s)) != cudaSuccess) return e;
@@ -190,7 +193,13 @@ cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEve
     if ((e = mark(3)) != cudaSuccess) return e;
     if ((e = fl::launch_grid_prep(b, h->C, s)) != cudaSuccess) return e;
     if ((e = mark(4)) != cudaSuccess) return e;
-    if ((e = fl::launch_cg(b, h->L, s, h->prm.cg_precision == FL_CG_F64)) != cudaSuccess) return e;
+    if (p_replay) {
+        if ((e = cudaMemcpyAsync(b.p, p_replay, sizeof(float) * (size_t)h->C, cudaMemcpyDeviceToDevice, s)) !=
+            cudaSuccess)
+            return e;
+    } else if ((e = fl::launch_cg(b, h->L, s, h->prm.cg_precision == FL_CG_F64)) != cudaSuccess) {
+        return e;
+    }
     if ((e = mark(5)) != cudaSuccess) return e;
     if ((e = fl::launch_project(b, h->C, s)) != cudaSuccess) return e;
     if ((e = mark(6)) != cudaSuccess) return e;
@@ -944,6 +953,7 @@ struct fl_tape {
     DevBufs cg{};        // buffers of the adjoint pressure solve (cg.p holds lambda)
     DevParams hp_cg{};
     fl_stats last{};     // of the last adjoint pressure solve
+    bool adj_warm = false;  // start each adjoint solve from the previous lambda
 };
 
 extern "C" {
@@ -1011,8 +1021,9 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     b.cg_off = (uint32_t*)(base + o_poff);
     b.cg_x = (unsigned long long*)(base + o_cgx);
     // The exchange words start cleared (tags of an earlier owner of this
-    // memory must not match).
+    // memory must not match); lambda starts at zero for a warm start.
     if ((e = cudaMemsetAsync(b.cg_x, 0, cgx_words * sizeof(unsigned long long), h->stream)) != cudaSuccess ||
+        (e = cudaMemsetAsync(b.p, 0, sizeof(float) * C, h->stream)) != cudaSuccess ||
         (e = cudaStreamSynchronize(h->stream)) != cudaSuccess) {
         cudaFree(t->pool);
         delete t;
@@ -1036,6 +1047,14 @@ fl_status fl_tape_clear(fl_tape* t) {
     return FL_OK;
 }
 
+fl_status fl_tape_set_adjoint_warm_start(fl_tape* t, int enable) {
+    if (!t) return set_err(nullptr, FL_INVALID_ARG, "tape is NULL");
+    fl_handle* h = t->h;
+    t->adj_warm = enable != 0;
+    FL_CUDA(h, cudaMemsetAsync(t->cg.p, 0, sizeof(float) * (size_t)h->C, h->stream));
+    return FL_OK;
+}
+
 fl_status fl_tape_count(const fl_tape* t, uint32_t* n_out) {
     if (!t || !n_out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
     *n_out = t->count;
@@ -1048,11 +1067,12 @@ fl_status fl_tape_last_stats(const fl_tape* t, fl_stats* out) {
     return FL_OK;
 }
 
-fl_status fl_step_record(fl_handle* h, fl_tape* t) {
-    if (!h || !t || t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
-    if (t->count >= t->max_steps) return set_err(h, FL_INVALID_ARG, "tape is full");
-    fl_status s = fl_step(h, 1);
-    if (s != FL_OK) return s;
+}  // extern "C"
+
+namespace {
+
+// Append the step just enqueued on the handle to the tape.
+fl_status tape_append(fl_handle* h, fl_tape* t) {
     char* slot = t->slots + (size_t)t->count * t->slot_bytes;
     const size_t n = h->n;
     cudaStream_t st = h->stream;
@@ -1068,6 +1088,37 @@ fl_status fl_step_record(fl_handle* h, fl_tape* t) {
     }
     t->count++;
     return FL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+fl_status fl_step_record(fl_handle* h, fl_tape* t) {
+    if (!h || !t || t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
+    if (t->count >= t->max_steps) return set_err(h, FL_INVALID_ARG, "tape is full");
+    fl_status s = fl_step(h, 1);
+    if (s != FL_OK) return s;
+    return tape_append(h, t);
+}
+
+fl_status fl_copy_pressure_device(fl_handle* h, void* dst_dev) {
+    if (!h || !dst_dev) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    FL_CUDA(h, cudaMemcpyAsync(dst_dev, h->b.p, sizeof(float) * (size_t)h->C, cudaMemcpyDeviceToDevice, h->stream));
+    return FL_OK;
+}
+
+fl_status fl_step_replay(fl_handle* h, const void* pressure_dev, fl_tape* t) {
+    if (!h || !pressure_dev) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    if (t && t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
+    if (t && t->count >= t->max_steps) return set_err(h, FL_INVALID_ARG, "tape is full");
+    DevBufs b = h->b;
+    b.part_in = h->partA;
+    b.part_out = h->partA;
+    b.ids_in = h->idsA;
+    FL_CUDA(h, enqueue_step(h, b, h->stream, nullptr, (const float*)pressure_dev));
+    h->substeps++;
+    return t ? tape_append(h, t) : FL_OK;
 }
 
 fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, void* dL_din_dev, float* dL_dgrav,
@@ -1098,19 +1149,22 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     a.g_in = (float4*)dL_din_dev;
     a.lam = t->cg.p;
     a.rhs = t->rhs;
+    a.rhs_part = t->adj_warm ? t->cg.chunk_rr_df : nullptr;  // free until k_solve_init
     a.g_grav = t->g_grav;
     FL_CUDA(h, cudaMemsetAsync(t->g_grav, 0, 3 * sizeof(double), st));
     FL_CUDA(h, fl::launch_adj_g2p(a, h->L, st));
     FL_CUDA(h, fl::launch_adj_prhs(a, h->C, st));
-    // adjoint pressure solve: A lambda = dL/dp (cold start; k_solve_init's rhs
-    // is -scale*div, so scale = -1 passes dL/dp through unchanged)
+    // adjoint pressure solve: A lambda = dL/dp (k_solve_init's rhs is
+    // -scale*div, so scale = -1 passes dL/dp through unchanged).  Cold start:
+    // stop at |r| <= tol |r0| = tol |dL/dp|.  Warm start from the previous
+    // step's lambda: the same bound, as an absolute threshold from k_adj_thr.
     fl_params q;
     std::memset(&q, 0, sizeof(q));
     q.gdim[0] = h->nx; q.gdim[1] = h->ny; q.gdim[2] = h->nz;
     q.geom[0] = h->prm.geom[0]; q.geom[1] = h->prm.geom[1]; q.geom[2] = h->prm.geom[2]; q.geom[3] = h->prm.geom[3];
     q.phys[1] = h->prm.phys[1];
     q.dims[2] = adj_cg_iters ? adj_cg_iters : 1u;
-    q.dims[3] = 0;
+    q.dims[3] = t->adj_warm ? 1u : 0u;
     q.pressure_tolerance = adj_cg_tol;
     q.cg_precision = h->prm.cg_precision;
     derive(q, h->n, t->hp_cg);
@@ -1119,6 +1173,7 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     cg.ct = const_cast<uint8_t*>(a.ct);
     FL_CUDA(h, cudaMemcpyAsync((void*)cg.prm, &t->hp_cg, sizeof(DevParams), cudaMemcpyHostToDevice, st));
     FL_CUDA(h, cudaMemsetAsync(cg.st, 0, sizeof(DevStats), st));
+    if (t->adj_warm) FL_CUDA(h, fl::launch_adj_thr(a, h->nchunks, t->hp_cg.tol_sq_d, (DevParams*)cg.prm, st));
     FL_CUDA(h, fl::launch_solve_init(cg, h->C, t->rhs, st));
     FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
     FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));

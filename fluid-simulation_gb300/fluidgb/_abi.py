@@ -128,9 +128,12 @@ SIGNATURES = {
     "fl_tape_create": (ctypes.c_int, [ctypes.c_void_p, c_u32, ctypes.POINTER(ctypes.c_void_p)]),
     "fl_tape_free": (ctypes.c_int, [ctypes.c_void_p]),
     "fl_tape_clear": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_tape_set_adjoint_warm_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fl_tape_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32)]),
     "fl_tape_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fl_step_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_copy_pressure_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "fl_step_replay": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "fl_step_adjoint": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _fp, c_u32,
                                        c_f32]),
     "fl_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
@@ -386,6 +389,15 @@ class Fluid:
         self._c(self.lib.fl_save_state(self.h, None, ctypes.byref(size)))
         return size.value
 
+    def copy_pressure_device(self, ptr):
+        """Pressure of the last substep (nx*ny*nz float32) into device memory at ptr."""
+        self._c(self.lib.fl_copy_pressure_device(self.h, ctypes.c_void_p(ptr)))
+
+    def step_replay(self, pressure_ptr, tape=None):
+        """One substep with the pressure solve replaced by the field at pressure_ptr
+        (recorded on `tape` when given)."""
+        self._c(self.lib.fl_step_replay(self.h, ctypes.c_void_p(pressure_ptr), tape.t if tape is not None else None))
+
     def save_state_device(self, ptr, size):
         sz = ctypes.c_size_t(size)
         self._c(self.lib.fl_save_state_device(self.h, ctypes.c_void_p(ptr), ctypes.byref(sz)))
@@ -433,6 +445,10 @@ class Tape:
 
     def clear(self):
         self.fluid._c(self.fluid.lib.fl_tape_clear(self.t))
+
+    def set_adjoint_warm_start(self, enable):
+        """Start each adjoint solve from the previous one's lambda (resets lambda to zero)."""
+        self.fluid._c(self.fluid.lib.fl_tape_set_adjoint_warm_start(self.t, 1 if enable else 0))
 
     def __len__(self):
         n = c_u32()

@@ -11,6 +11,16 @@ forward), then popped step by step through the adjoint kernels.  Memory: one
 tape of `checkpoint_every` substeps plus the checkpoints; nothing leaves the
 GPU.  With checkpoint_every >= steps nothing is recomputed.
 
+With pressure_log (the default) the forward also keeps every substep's
+pressure field (4 bytes per cell per substep), and the recomputation replays
+each substep with that field in place of its CG (fl_step_replay): the same
+bits, without the solve that dominates the substep.
+
+Each adjoint pressure solve starts, by default, from the adjoint pressure of
+the step after it (the one solved just before in the backward walk) and stops
+at the cold start's bound |r| <= tol |dL/dp| (fl_tape_set_adjoint_warm_start);
+adj_warm_start=False starts every solve from zero.
+
 Gradients are taken with respect to the initial per-particle state and the
 gravity (body-force) vector, as in the differentiable-rollout workload:
 `loss = |mean(final positions) - target|^2`, d loss / d(initial velocity, gravity).
@@ -36,7 +46,8 @@ class Rollout:
     CUDA device; the handle runs on a stream of its own, ordered against the
     caller's stream at entry and exit."""
 
-    def __init__(self, params, capacity, steps, checkpoint_every=10, adj_cg_iters=1000, adj_cg_tol=1e-6):
+    def __init__(self, params, capacity, steps, checkpoint_every=10, adj_cg_iters=1000, adj_cg_tol=1e-6,
+                 adj_warm_start=True, pressure_log=True):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.stream = torch.cuda.Stream(self.dev)
         self.fluid = Fluid(params, capacity)
@@ -46,6 +57,9 @@ class Rollout:
         self.k = max(1, int(checkpoint_every))
         self.adj_cg_iters = adj_cg_iters
         self.adj_cg_tol = adj_cg_tol
+        self.adj_warm_start = bool(adj_warm_start)
+        self.cells = int(params.gdim[0]) * int(params.gdim[1]) * int(params.gdim[2])
+        self.plog = torch.empty((self.steps, self.cells), dtype=torch.float32, device=self.dev) if pressure_log else None
         self.tape = self.fluid.tape(self.k)
         self.checkpoints = {}
         self.taped = None
@@ -92,6 +106,8 @@ class Rollout:
                     self.tape.record()
                 else:
                     self.fluid.step(1)
+                if self.plog is not None:
+                    self.fluid.copy_pressure_device(self.plog[s].data_ptr())
             self.taped = last
             for s in [s for s in self.checkpoints if s >= self.steps or s % self.k]:
                 del self.checkpoints[s]
@@ -110,14 +126,18 @@ class Rollout:
         with self._enter():
             g_out = _as_device_particles(g_final, self.dev).clone()
             g_in = torch.empty_like(g_out)
+            self.tape.set_adjoint_warm_start(self.adj_warm_start)
             for s0 in sorted(self.checkpoints, reverse=True):
                 s1 = min(s0 + self.k, self.steps)
                 if s0 != self.taped or len(self.tape) != s1 - s0:
                     buf = self.checkpoints[s0]
                     self.fluid.load_state_device(buf.data_ptr(), buf.numel())
                     self.tape.clear()
-                    for _ in range(s0, s1):
-                        self.tape.record()
+                    for s in range(s0, s1):
+                        if self.plog is not None:
+                            self.fluid.step_replay(self.plog[s].data_ptr(), self.tape)
+                        else:
+                            self.tape.record()
                 self.taped = None
                 for _ in range(s0, s1):
                     gg = self.tape.adjoint(g_out.data_ptr(), g_in.data_ptr(), self.adj_cg_iters, self.adj_cg_tol)

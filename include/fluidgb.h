@@ -209,11 +209,28 @@ typedef struct fl_tape fl_tape;
 fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out);
 fl_status fl_tape_free(fl_tape* t);
 fl_status fl_tape_clear(fl_tape* t);
+/* Warm start of the adjoint pressure solve (off after fl_tape_create).  When
+ * on, each fl_step_adjoint starts its CG from the adjoint pressure of the
+ * previous call instead of zero, and stops once |r| <= adj_cg_tol * |dL/dp|
+ * (the bound the cold start's relative test gives) or at adj_cg_iters.  Every
+ * call, on or off, resets the carried adjoint pressure to zero: a backward
+ * pass that begins with it does not depend on earlier ones. */
+fl_status fl_tape_set_adjoint_warm_start(fl_tape* t, int enable);
 fl_status fl_tape_count(const fl_tape* t, uint32_t* n_out);
 fl_status fl_tape_last_stats(const fl_tape* t, fl_stats* out);
 fl_status fl_step_record(fl_handle* h, fl_tape* t);
 fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, void* dL_din_dev, float* dL_dgrav,
                           uint32_t adj_cg_iters, float adj_cg_tol);
+
+/* ---- pressure log (rollouts that recompute without the pressure solve) ----
+ * fl_copy_pressure_device copies the pressure field of the last substep
+ * (C = nx*ny*nz floats, x fastest) to device memory.  fl_step_replay runs one
+ * substep like fl_step(h, 1) with the pressure solve replaced by
+ * `pressure_dev`: given the field that the same substep's solve produced, the
+ * substep is reproduced bit for bit without its CG.  With a tape (not NULL)
+ * the substep is also recorded, as by fl_step_record. */
+fl_status fl_copy_pressure_device(fl_handle* h, void* dst_dev);
+fl_status fl_step_replay(fl_handle* h, const void* pressure_dev, fl_tape* t);
 
 /* Per-stage device time, measured with CUDA events on the handle's stream
  * (the sections of the reference's GpuTimers, gpu/timing.rs:32-59, grouped by

@@ -120,7 +120,38 @@ def test_checkpointed_recompute_matches_forward():
     # the device checkpoint holds the same bytes as the host one
     roll.fluid.load_state_device(buf.data_ptr(), buf.numel())
     assert roll.fluid.save_state() == bytes(buf.cpu().numpy())
+    # replaying every substep from the start with the logged pressure fields
+    # (no CG) reproduces the forward bit for bit
+    buf = roll.checkpoints[0]
+    roll.fluid.load_state_device(buf.data_ptr(), buf.numel())
+    for s in range(steps):
+        roll.fluid.step_replay(roll.plog[s].data_ptr())
+    again, ids2 = roll.fluid.get_particles()
+    assert np.array_equal(final.cpu().numpy(), again) and np.array_equal(ids.cpu().numpy(), ids2)
     roll.close()
+
+
+def test_pressure_log_recompute_gives_the_same_gradients():
+    """Backward passes that recompute segments by replaying logged pressure
+    fields and by re-solving agree (to the last-bit noise of the face
+    scatters' float atomics)."""
+    torch = pytest.importorskip("torch")
+    from fluidgb.autograd import Rollout
+    p, parts, steps = setup_case(steps=9)
+    n = parts.shape[0]
+    g = np.zeros((n, 8), np.float32)
+    g[:, 0:3] = np.random.default_rng(6).standard_normal((n, 3)).astype(np.float32) / n
+    out = []
+    for plog in (False, True):
+        roll = Rollout(p, n, steps, checkpoint_every=3, adj_cg_iters=500, adj_cg_tol=1e-6, pressure_log=plog)
+        final, ids = roll.forward(parts, (0.0, -9.81, 0.0))
+        g0, gg = roll.backward(torch.from_numpy(g).cuda()[ids])
+        out.append((g0.cpu().numpy().copy(), np.asarray(gg).copy()))
+        roll.close()
+    rel = np.linalg.norm(out[1][0] - out[0][0]) / np.linalg.norm(out[0][0])
+    relg = np.linalg.norm(out[1][1] - out[0][1]) / np.linalg.norm(out[0][1])
+    print("pressure log vs re-solve: gradient rel. difference %.1e (particles), %.1e (gravity)" % (rel, relg))
+    assert rel < 1e-5 and relg < 1e-5
 
 
 @pytest.mark.parametrize("steps,k,what", [(1, 1, "pos"), (2, 1, "vel"), (4, 4, "vel"), (4, 2, "grav")])
@@ -168,3 +199,39 @@ def test_adjoint_position_and_chain_diagnostics(oracle, steps, k, what):
         oracle.set_exact_p2g(False)
     print("%s steps %d k %d: adjoint %.6e fd %.6e rel %.2e" % (what, steps, k, ad, fd, abs(ad - fd) / abs(fd)))
     assert abs(ad - fd) <= 1e-2 * abs(fd)
+
+
+def test_adjoint_warm_start_matches_cold_start():
+    """The warm-started adjoint solve (each from the next step's lambda, same
+    |r| <= tol |dL/dp| bound) gives the cold start's gradients to the solve's
+    tolerance in fewer CG iterations, and a second backward pass repeats the
+    first (lambda is reset at its start; the face scatters' float atomics
+    leave last-bit differences, so the repeat is compared to 1e-5)."""
+    torch = pytest.importorskip("torch")
+    from fluidgb.autograd import Rollout
+    p = scenes.params_for(32, iters=400, tol=1e-6, precision=FL_CG_F64, stiffness=0.0)
+    parts = scenes.seed_particles(32, scenes.box(0.5, 0.4), vel_sigma=0.1)
+    n, steps = parts.shape[0], 20
+    g = np.zeros((n, 8), np.float32)
+    g[:, 0:3] = np.random.default_rng(5).standard_normal((n, 3)).astype(np.float32) / n
+
+    def grads(warm):
+        roll = Rollout(p, n, steps, checkpoint_every=5, adj_cg_iters=400, adj_cg_tol=1e-6, adj_warm_start=warm)
+        final, ids = roll.forward(parts, (0.0, -9.81, 0.0))
+        gf = torch.from_numpy(g).cuda()[ids]
+        g0, gg = roll.backward(gf)
+        out = (g0.cpu().numpy().copy(), np.asarray(gg).copy(), list(roll.adj_cg_iterations))
+        g1, _ = roll.backward(gf)
+        rep = np.linalg.norm(g1.cpu().numpy() - out[0]) / np.linalg.norm(out[0])
+        roll.close()
+        return out + (rep,)
+
+    gc, ggc, itc, repc = grads(False)
+    gw, ggw, itw, repw = grads(True)
+    rel = np.linalg.norm(gw - gc) / np.linalg.norm(gc)
+    relg = np.linalg.norm(ggw - ggc) / np.linalg.norm(ggc)
+    print("adjoint CG iterations: cold %d, warm %d; gradient rel. difference %.2e (particles), %.2e (gravity); "
+          "repeat %.1e (cold) %.1e (warm)" % (sum(itc), sum(itw), rel, relg, repc, repw))
+    assert repc < 1e-5 and repw < 1e-5
+    assert sum(itw) < sum(itc)
+    assert rel < 1e-3 and relg < 1e-3

@@ -187,15 +187,6 @@ __device__ __forceinline__ float chunk_tree(const float* s, uint32_t lane) {
 // quotients rounded to f32, and the stopping test compares float-float values.
 
 // a / b rounded to f32: the f32 quotient plus one float-float correction.
-__device__ __forceinline__ float df_div(Df a, Df b) {
-    const float q1 = __fdiv_rn(a.hi, b.hi);
-    const float p = __fmul_rn(q1, b.hi);
-    const float pe = __fmaf_rn(q1, b.hi, -p);  // q1*b.hi - p, exact
-    const float r = __fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), __fmul_rn(q1, b.lo)), a.lo);
-    return __fadd_rn(q1, __fdiv_rn(r, b.hi));
-}
-__device__ __forceinline__ bool df_le(Df a, Df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
-__device__ __forceinline__ double df_to_double(Df a) { return (double)a.hi + (double)a.lo; }
 
 // ---------------------------------------------------------------------------
 // Plan
@@ -767,6 +758,12 @@ int cg_max_blocks_per_sm() {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n[i], f, CG_THREADS, sizeof(CgShared)) != cudaSuccess) return 0;
     }
     return n[0] < n[1] ? n[0] : n[1];
+}
+
+cudaError_t launch_cg_plan(const DevBufs& b, uint32_t G, cudaStream_t s) {
+    if (G < 1 || G > MAX_CG_BLOCKS) return cudaErrorInvalidValue;
+    k_cg_plan<<<1, CHUNK, 0, s>>>(b, G);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, bool f64) {

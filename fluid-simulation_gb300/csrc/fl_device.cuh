@@ -36,7 +36,7 @@ struct DevParams {
     float lo[3], half_dt;                // origin + h*1.05 (g2p.wgsl:166)
     float hi[3], pad0;                   // origin + extent - h*1.05 (g2p.wgsl:167)
     uint32_t thresh, dilation, warm, iters;
-    uint32_t precision, advect_order, nchunks, pad1;
+    uint32_t precision, advect_order, nchunks, solver;  // solver: FL_SOLVER_*
     double tol_sq_d;
     // Absolute stopping threshold on r.r, used instead of tol^2 * (r0.r0) when
     // thr_abs is 1 (the warm-started adjoint solve: tol^2 * |rhs|^2, written
@@ -181,6 +181,17 @@ __device__ __forceinline__ Df warp_allsum_df(Df v) {  // result in every lane
     return v;
 }
 
+// a/b to f32 precision from float-float operands (one Newton correction).
+__device__ __forceinline__ float df_div(Df a, Df b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const float p = __fmul_rn(q1, b.hi);
+    const float pe = __fmaf_rn(q1, b.hi, -p);  // q1*b.hi - p, exact
+    const float r = __fadd_rn(__fsub_rn(__fsub_rn(__fsub_rn(a.hi, p), pe), __fmul_rn(q1, b.lo)), a.lo);
+    return __fadd_rn(q1, __fdiv_rn(r, b.hi));
+}
+__device__ __forceinline__ bool df_le(Df a, Df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo <= b.lo); }
+__device__ __forceinline__ double df_to_double(Df a) { return (double)a.hi + (double)a.lo; }
+
 __device__ __forceinline__ uint32_t face_dim(const DevParams& P, int axis, int b) {
     uint32_t n = b == 0 ? P.nx : (b == 1 ? P.ny : P.nz);
     return n + (axis == b ? 1u : 0u);
@@ -281,6 +292,39 @@ struct SeedArgs {
 long long seed_layout(const fl_params& prm, const fl_block* blocks, uint32_t nblocks, uint32_t particle_count,
                       SeedArgs* out);
 cudaError_t launch_seed(const SeedArgs& a, float4* part, cudaStream_t s);
+// Multigrid hierarchy of the MGPCG solver (fl_mg.cu).  Level 0 is the grid
+// (its operator comes from cinfo; b = the CG residual r, x = z = M^-1 r);
+// level l+1 aggregates 2x2x2 cells of level l.
+constexpr int MG_MAX_LEVELS = 12;
+constexpr uint32_t MG_COARSE_CELLS = 64;  // the coarsest level holds at most this many cells
+struct MgLevel {
+    uint32_t nx, ny, nz, C;
+    float4* st;  // {diag, weight to +x, +y, +z} (levels >= 1)
+    float* b;
+    float* x;
+};
+struct MgBufs {
+    uint32_t L;         // number of levels (>= 2)
+    MgLevel lv[MG_MAX_LEVELS];
+    float2* part;       // 2 x MAX_CG_BLOCKS float-float block partials
+    uint32_t* bar;      // barrier counter, zeroed before each solve
+};
+// Level sizes of an nx x ny x nz grid; returns L.
+FL_HD inline uint32_t mg_levels(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t dims[MG_MAX_LEVELS][3]) {
+    uint32_t L = 0;
+    for (;;) {
+        dims[L][0] = nx; dims[L][1] = ny; dims[L][2] = nz;
+        L++;
+        if ((size_t)nx * ny * nz <= MG_COARSE_CELLS || L == MG_MAX_LEVELS) break;
+        nx = (nx + 1) / 2; ny = (ny + 1) / 2; nz = (nz + 1) / 2;
+    }
+    return L;
+}
+// The CG's plan of active chunks split over G blocks (fl_cg.cu).
+cudaError_t launch_cg_plan(const DevBufs& b, uint32_t G, cudaStream_t s);
+cudaError_t launch_mgpcg(const DevBufs& b, const MgBufs& m, const LaunchCfg& L, cudaStream_t s);
+int mg_max_blocks_per_sm();
+
 struct AdjBufs;
 cudaError_t launch_adj_g2p(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s);

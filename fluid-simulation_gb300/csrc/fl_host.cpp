@@ -51,6 +51,8 @@ struct fl_handle {
     uint32_t init_n = 0;
     uint64_t substeps = 0;
     float4* slice_buf = nullptr;  // device staging of fl_grid_slice (nx*ny float4), allocated on first use
+    fl::MgBufs mg{};              // MGPCG hierarchy, allocated when that solver is first selected
+    void* mg_pool = nullptr;
     std::string err;
 };
 
@@ -92,7 +94,8 @@ fl_status validate(const fl_params* p, std::string* why) {
     if (!(p->phys[1] > 0.0f)) { *why = "rho must be > 0"; return FL_INVALID_ARG; }
     if (p->cg_precision > 1u) { *why = "cg_precision must be FL_CG_F32 or FL_CG_F64"; return FL_INVALID_ARG; }
     if (p->advect_order > 2u) { *why = "advect_order must be 1 or 2"; return FL_INVALID_ARG; }
-    for (int i = 0; i < 4; i++)
+    if (p->pressure_solver > 1u) { *why = "pressure_solver must be FL_SOLVER_CG or FL_SOLVER_MGPCG"; return FL_INVALID_ARG; }
+    for (int i = 0; i < 3; i++)
         if (p->reserved[i]) { *why = "reserved fields must be zero"; return FL_INVALID_ARG; }
     return FL_OK;
 }
@@ -131,6 +134,7 @@ void derive(const fl_params& p, uint32_t n, DevParams& d) {
     d.precision = p.cg_precision;
     d.advect_order = p.advect_order == 2u ? 2u : 1u;
     d.nchunks = (d.C + fl::CHUNK - 1) / fl::CHUNK;
+    d.solver = p.pressure_solver;
 }
 
 struct PoolPlan {
@@ -146,6 +150,50 @@ struct PoolPlan {
 
 int g_num_sms = -1;
 int g_cg_per_sm = 0;
+
+// Multigrid hierarchy of an nx x ny x nz grid in one device pool: per level
+// l >= 1 the float4 stencil, b and x; z of level 0; the block partials and the
+// barrier counter.  Level 0's b is the solve's residual r.
+fl_status mg_alloc(fl_handle* h, uint32_t nx, uint32_t ny, uint32_t nz, float* r, fl::MgBufs* m, void** pool) {
+    if (*pool) return FL_OK;
+    uint32_t dims[fl::MG_MAX_LEVELS][3];
+    const uint32_t L = fl::mg_levels(nx, ny, nz, dims);
+    if (L < 2 || (size_t)dims[L - 1][0] * dims[L - 1][1] * dims[L - 1][2] > fl::MG_COARSE_CELLS)
+        return set_err(h, FL_INVALID_ARG, "grid too small or too large for the multigrid hierarchy");
+    if (fl::mg_max_blocks_per_sm() < 1) return set_err(h, FL_INTERNAL, "MGPCG kernel cannot be resident");
+    PoolPlan pl;
+    size_t o_st[fl::MG_MAX_LEVELS] = {}, o_b[fl::MG_MAX_LEVELS] = {}, o_x[fl::MG_MAX_LEVELS] = {};
+    for (uint32_t l = 0; l < L; l++) {
+        const size_t C = (size_t)dims[l][0] * dims[l][1] * dims[l][2];
+        if (l > 0) {
+            o_st[l] = pl.take<float4>(C);
+            o_b[l] = pl.take<float>(C);
+        }
+        o_x[l] = pl.take<float>(C);
+    }
+    const size_t o_part = pl.take<float2>(2 * 1024), o_bar = pl.take<uint32_t>(1);
+    void* base = nullptr;
+    cudaError_t e = cudaMalloc(&base, pl.off);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return set_err(h, FL_OOM, "multigrid allocation of " + std::to_string(pl.off) + " bytes failed");
+    }
+    char* c = (char*)base;
+    *m = fl::MgBufs{};
+    m->L = L;
+    for (uint32_t l = 0; l < L; l++) {
+        fl::MgLevel& lv = m->lv[l];
+        lv.nx = dims[l][0]; lv.ny = dims[l][1]; lv.nz = dims[l][2];
+        lv.C = lv.nx * lv.ny * lv.nz;
+        lv.st = l ? (float4*)(c + o_st[l]) : nullptr;
+        lv.b = l ? (float*)(c + o_b[l]) : r;
+        lv.x = (float*)(c + o_x[l]);
+    }
+    m->part = (float2*)(c + o_part);
+    m->bar = (uint32_t*)(c + o_bar);
+    *pool = base;
+    return FL_OK;
+}
 
 fl_status device_check(fl_handle* h) {
     int dev = 0;
@@ -197,6 +245,8 @@ cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEve
         if ((e = cudaMemcpyAsync(b.p, p_replay, sizeof(float) * (size_t)h->C, cudaMemcpyDeviceToDevice, s)) !=
             cudaSuccess)
             return e;
+    } else if (h->prm.pressure_solver == FL_SOLVER_MGPCG) {
+        if ((e = fl::launch_mgpcg(b, h->mg, h->L, s)) != cudaSuccess) return e;
     } else if ((e = fl::launch_cg(b, h->L, s, h->prm.cg_precision == FL_CG_F64)) != cudaSuccess) {
         return e;
     }
@@ -409,6 +459,12 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     b.cg_chunk = (uint32_t*)(base + o_plan);
     b.cg_off = (uint32_t*)(base + o_poff);
     b.cg_x = (unsigned long long*)(base + o_cgx);
+    if (params->pressure_solver == FL_SOLVER_MGPCG &&
+        (s = mg_alloc(h, h->nx, h->ny, h->nz, b.r, &h->mg, &h->mg_pool)) != FL_OK) {
+        std::string m = h->err;
+        fl_destroy(h);
+        return set_err(nullptr, s, m);
+    }
     if ((s = upload_params(h)) != FL_OK) {
         std::string m = h->err;
         fl_destroy(h);
@@ -427,6 +483,7 @@ fl_status fl_destroy(fl_handle* h) {
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     if (h->pool) cudaFree(h->pool);
     if (h->slice_buf) cudaFree(h->slice_buf);
+    if (h->mg_pool) cudaFree(h->mg_pool);
     delete h;
     return FL_OK;
 }
@@ -437,8 +494,13 @@ fl_status fl_set_params(fl_handle* h, const fl_params* params) {
     if (validate(params, &why) != FL_OK) return set_err(h, FL_INVALID_ARG, why);
     if (params->gdim[0] != h->nx || params->gdim[1] != h->ny || params->gdim[2] != h->nz)
         return set_err(h, FL_INVALID_ARG, "grid dimensions cannot change on a live handle; create a new one");
-    if (params->cg_precision != h->prm.cg_precision && h->graph) {
-        // the CG kernel is specialised per precision: capture the step again
+    if (params->pressure_solver == FL_SOLVER_MGPCG) {
+        fl_status s = mg_alloc(h, h->nx, h->ny, h->nz, h->b.r, &h->mg, &h->mg_pool);
+        if (s != FL_OK) return s;
+    }
+    if ((params->cg_precision != h->prm.cg_precision || params->pressure_solver != h->prm.pressure_solver) &&
+        h->graph) {
+        // the solver kernels differ per precision and solver: capture the step again
         FL_CUDA(h, cudaStreamSynchronize(h->stream));
         cudaGraphExecDestroy(h->graph);
         h->graph = nullptr;

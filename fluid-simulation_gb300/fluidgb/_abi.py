@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libfluidgb.so")
 FL_OK, FL_INVALID_ARG, FL_OOM, FL_CUDA_ERROR, FL_NOT_CONVERGED, FL_TIMEOUT, FL_NO_DEVICE, FL_INTERNAL = range(8)
 FL_CELL_SOLID, FL_CELL_LIQUID, FL_CELL_AIR = 0, 1, 2
 FL_CG_F32, FL_CG_F64 = 0, 1
+FL_SOLVER_CG, FL_SOLVER_MGPCG = 0, 1
 
 c_u32 = ctypes.c_uint32
 c_f32 = ctypes.c_float
@@ -28,7 +29,7 @@ class FlParams(ctypes.Structure):
         ("dims", c_u32 * 4), ("geom", c_f32 * 4), ("phys", c_f32 * 4), ("origin", c_f32 * 4),
         ("grav", c_f32 * 4), ("spc", c_f32 * 4), ("cls", c_f32 * 4), ("gdim", c_u32 * 4),
         ("pressure_tolerance", c_f32), ("cg_precision", c_u32), ("advect_order", c_u32),
-        ("sort_period", c_u32), ("reserved", c_u32 * 4),
+        ("sort_period", c_u32), ("pressure_solver", c_u32), ("reserved", c_u32 * 3),
     ]
 
     def copy(self):

@@ -80,8 +80,18 @@ typedef struct fl_params {
     uint32_t advect_order;    /* 1 = forward Euler (reference g2p.wgsl:186); 2 = midpoint */
     uint32_t sort_period;     /* accepted for drop-in compatibility; the layout is
                                  re-sorted every substep (the gather-form P2G reads bins) */
-    uint32_t reserved[4];     /* must be zero */
+    uint32_t pressure_solver; /* FL_SOLVER_CG (the reference's CG) or FL_SOLVER_MGPCG */
+    uint32_t reserved[3];     /* must be zero */
 } fl_params;
+
+/* Pressure solvers.  FL_SOLVER_CG is the reference's CG (cg_*.wgsl).
+ * FL_SOLVER_MGPCG preconditions the same CG with a multigrid V-cycle whose
+ * smoother is the reference's red-black Gauss-Seidel sweep (pressure.wgsl):
+ * same operator, warm start, iteration cap and stopping test, far fewer
+ * iterations; the pressure agrees with the CG's to the tolerance, not bit for
+ * bit.  Reductions are float-float in both precisions. */
+#define FL_SOLVER_CG 0u
+#define FL_SOLVER_MGPCG 1u
 
 typedef struct fl_handle fl_handle;
 

@@ -297,6 +297,8 @@ cudaError_t launch_seed(const SeedArgs& a, float4* part, cudaStream_t s);
 // level l+1 aggregates 2x2x2 cells of level l.
 constexpr int MG_MAX_LEVELS = 12;
 constexpr uint32_t MG_COARSE_CELLS = 64;  // the coarsest level holds at most this many cells
+constexpr uint32_t MG_BLOCK0_CELLS = 4096;  // levels this small run inside one block (block barriers)
+constexpr uint32_t MG_LOCAL_TOTAL = 4800;   // cells of all those levels together (b, x in shared memory)
 struct MgLevel {
     uint32_t nx, ny, nz, C;
     float4* st;  // {diag, weight to +x, +y, +z} (levels >= 1)
@@ -306,6 +308,7 @@ struct MgLevel {
 struct MgBufs {
     uint32_t L;         // number of levels (>= 2)
     MgLevel lv[MG_MAX_LEVELS];
+    float* r2;          // second residual buffer (level-0 size)
     float2* part;       // 2 x MAX_CG_BLOCKS float-float block partials
     uint32_t* bar;      // barrier counter, zeroed before each solve
 };

@@ -160,6 +160,17 @@ fl_status mg_alloc(fl_handle* h, uint32_t nx, uint32_t ny, uint32_t nz, float* r
     const uint32_t L = fl::mg_levels(nx, ny, nz, dims);
     if (L < 2 || (size_t)dims[L - 1][0] * dims[L - 1][1] * dims[L - 1][2] > fl::MG_COARSE_CELLS)
         return set_err(h, FL_INVALID_ARG, "grid too small or too large for the multigrid hierarchy");
+    {
+        // the levels from the first one of at most MG_BLOCK0_CELLS cells on run
+        // in one block, their vectors in its shared memory
+        auto cells = [&](uint32_t l) { return (size_t)dims[l][0] * dims[l][1] * dims[l][2]; };
+        uint32_t Lg = 1;
+        while (Lg + 1 < L && cells(Lg) > fl::MG_BLOCK0_CELLS) Lg++;
+        size_t local = 0;
+        for (uint32_t l = Lg; l < L; l++) local += cells(l);
+        if (local > fl::MG_LOCAL_TOTAL)
+            return set_err(h, FL_INVALID_ARG, "grid shape unsupported by the multigrid solver (coarse levels too elongated)");
+    }
     if (fl::mg_max_blocks_per_sm() < 1) return set_err(h, FL_INTERNAL, "MGPCG kernel cannot be resident");
     PoolPlan pl;
     size_t o_st[fl::MG_MAX_LEVELS] = {}, o_b[fl::MG_MAX_LEVELS] = {}, o_x[fl::MG_MAX_LEVELS] = {};
@@ -171,6 +182,7 @@ fl_status mg_alloc(fl_handle* h, uint32_t nx, uint32_t ny, uint32_t nz, float* r
         }
         o_x[l] = pl.take<float>(C);
     }
+    const size_t o_r2 = pl.take<float>((size_t)nx * ny * nz);
     const size_t o_part = pl.take<float2>(2 * 1024), o_bar = pl.take<uint32_t>(1);
     void* base = nullptr;
     cudaError_t e = cudaMalloc(&base, pl.off);
@@ -189,6 +201,7 @@ fl_status mg_alloc(fl_handle* h, uint32_t nx, uint32_t ny, uint32_t nz, float* r
         lv.b = l ? (float*)(c + o_b[l]) : r;
         lv.x = (float*)(c + o_x[l]);
     }
+    m->r2 = (float*)(c + o_r2);
     m->part = (float2*)(c + o_part);
     m->bar = (uint32_t*)(c + o_bar);
     *pool = base;

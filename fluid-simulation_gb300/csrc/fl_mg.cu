@@ -44,38 +44,53 @@ namespace fl {
 namespace {
 
 constexpr int MG_THREADS = 1024;
-constexpr int MG_PART = 1024;       // block partial slots per exchange parity
-constexpr int MG_KCH = 2048;        // level-0 plan entries cached in shared memory
-constexpr int MG_COARSE_SWEEPS = 8;  // symmetric Gauss-Seidel sweeps on the coarsest level
+constexpr int MG_PART = 1024;             // block partial slots per exchange parity
+constexpr int MG_CELLS = 20480;           // level-0 unknowns listed per block
+constexpr int MG_L1 = 4096;               // level-1 unknowns listed per block
+constexpr int MG_COARSE_SWEEPS = 2;       // symmetric Gauss-Seidel sweeps on the coarsest level
+constexpr int MG_BATCH = 1;               // level-0 cells per thread whose loads are issued together
+
+// Level-0 cell metadata: bits 0-9 the CG's stencil mask (bit 0 liquid, bit
+// s+1 neighbour s of -x,+x,-y,+y,-z,+z liquid, bits 7-9 the non-solid count),
+// bits 10-12 the parities of i, j, k, bit 13 the colour (i+j+k)&1 (0 = red).
+constexpr uint32_t META_IODD = 1u << 10, META_JODD = 1u << 11, META_KODD = 1u << 12, META_BLACK = 1u << 13;
 
 struct MgShared {
-    uint32_t chunk[MG_KCH];
+    uint32_t cell[MG_CELLS];
+    uint16_t meta[MG_CELLS];
+    uint32_t l1[MG_L1];
+    float lb[MG_LOCAL_TOTAL], lx[MG_LOCAL_TOTAL];  // b and x of the levels block 0 runs alone
     float2 red[MG_THREADS / 32];
+    uint32_t wc[MG_THREADS / 32];
     float2 res;
     int ok;
-    float4 cst[MG_COARSE_CELLS];
-    float cb[MG_COARSE_CELLS], cx[MG_COARSE_CELLS];
+    uint32_t ncell, nl1, list0, list1;
+    // solve scalars kept here rather than in registers through the loop
+    float2 rs0, thr, rz;
 };
 
-__device__ __forceinline__ bool red_cell(uint32_t c, uint32_t nx, uint32_t ny) {
+__device__ __forceinline__ uint32_t make_meta(uint32_t info, uint32_t c, uint32_t nx, uint32_t ny) {
     const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-    return ((i + j + k) & 1u) == 0u;
+    return info | ((i & 1u) ? META_IODD : 0u) | ((j & 1u) ? META_JODD : 0u) | ((k & 1u) ? META_KODD : 0u) |
+           (((i + j + k) & 1u) ? META_BLACK : 0u);
 }
 
-// Level-0 operator from the CG's stencil mask: bit 0 liquid, bit s+1 the
-// neighbour s (-x,+x,-y,+y,-z,+z) is liquid, bits 7-9 the non-solid count.
-__device__ __forceinline__ float diag0(uint32_t info) { return (float)(info >> 7); }
+__device__ __forceinline__ float diag0(uint32_t meta) { return (float)((meta >> 7) & 7u); }
 
-// Sum over the liquid neighbours of v(nb).
+// Stencils and masks do not change during the solve: read-only cache.
+__device__ __forceinline__ float4 ld_st(const float4* st, uint32_t c) { return __ldg(st + c); }
+__device__ __forceinline__ uint32_t ld_ci(const uint16_t* ci, uint32_t c) { return __ldg(ci + c); }
+
+// Sum over the liquid neighbours of v(nb, side) (side 0..5 = -x,+x,-y,+y,-z,+z).
 template <class F>
-__device__ __forceinline__ float nbsum0(uint32_t info, uint32_t c, uint32_t nx, uint32_t nxy, F v) {
+__device__ __forceinline__ float nbsum0(uint32_t meta, uint32_t c, uint32_t nx, uint32_t nxy, F v) {
     float s = 0.0f;
-    if (info & (1u << 1)) s += v(c - 1);
-    if (info & (1u << 2)) s += v(c + 1);
-    if (info & (1u << 3)) s += v(c - nx);
-    if (info & (1u << 4)) s += v(c + nx);
-    if (info & (1u << 5)) s += v(c - nxy);
-    if (info & (1u << 6)) s += v(c + nxy);
+    if (meta & (1u << 1)) s += v(c - 1, 0);
+    if (meta & (1u << 2)) s += v(c + 1, 1);
+    if (meta & (1u << 3)) s += v(c - nx, 2);
+    if (meta & (1u << 4)) s += v(c + nx, 3);
+    if (meta & (1u << 5)) s += v(c - nxy, 4);
+    if (meta & (1u << 6)) s += v(c + nxy, 5);
     return s;
 }
 
@@ -90,15 +105,15 @@ __device__ __forceinline__ float nbsum(const float4* st, float4 sc, uint32_t c, 
     if (sc.z != 0.0f) s += sc.z * v(c + lv.nx);
     if (sc.w != 0.0f) s += sc.w * v(c + nxy);
     if (i > 0) {
-        const float w = st[c - 1].y;
+        const float w = ld_st(st, c - 1).y;
         if (w != 0.0f) s += w * v(c - 1);
     }
     if (j > 0) {
-        const float w = st[c - lv.nx].z;
+        const float w = ld_st(st, c - lv.nx).z;
         if (w != 0.0f) s += w * v(c - lv.nx);
     }
     if (k > 0) {
-        const float w = st[c - nxy].w;
+        const float w = ld_st(st, c - nxy).w;
         if (w != 0.0f) s += w * v(c - nxy);
     }
     return s;
@@ -113,16 +128,17 @@ struct Ctx {
     MgShared& sh;
     const DevBufs& b;
     const MgBufs& m;
-    uint32_t nown;      // level-0 plan entries of this block
-    uint32_t e0;        // first one (when not cached)
+    uint32_t e0, nown;  // this block's level-0 plan entries
+    uint32_t Lg;        // first level run inside block 0 alone (>= 1)
+    const float* r;     // the current residual (level 0's b)
     uint32_t epoch;     // barrier target
     uint32_t parity;    // exchange slot parity
 };
 
 __device__ bool mg_barrier(Ctx& x) {
     __syncthreads();
+    x.epoch += gridDim.x;
     if (threadIdx.x == 0) {
-        x.epoch += gridDim.x;
         __threadfence();
         red_release_add(x.m.bar, 1u);
         bool ok = true;
@@ -142,8 +158,6 @@ __device__ bool mg_barrier(Ctx& x) {
             }
         }
         x.sh.ok = ok;
-    } else {
-        x.epoch += gridDim.x;
     }
     __syncthreads();
     return x.sh.ok != 0;
@@ -165,9 +179,15 @@ __device__ bool mg_allreduce(Ctx& x, Df v, Df& out) {
     if (!mg_barrier(x)) return false;
     if (warp == 0) {
         Df s = {0.0f, 0.0f};
-        for (uint32_t g = lane; g < gridDim.x; g += 32) {
-            const float2 p = part[g];
-            s = df_add(s, Df{p.x, p.y});
+        for (uint32_t g0 = 0; g0 < gridDim.x; g0 += 8 * 32) {
+            float2 p[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const uint32_t g = g0 + lane + 32u * k;
+                p[k] = g < gridDim.x ? part[g] : make_float2(0.0f, 0.0f);
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) s = df_add(s, Df{p[k].x, p[k].y});
         }
         s = warp_allsum_df(s);
         if (lane == 0) x.sh.res = make_float2(s.hi, s.lo);
@@ -177,140 +197,340 @@ __device__ bool mg_allreduce(Ctx& x, Df v, Df& out) {
     return true;
 }
 
-// Calls f(c, info) for every liquid cell of this block's level-0 plan entries.
+// Position of this thread's item among the flagged items of the block (in
+// thread order) and their total; uses sh.wc.
+__device__ __forceinline__ uint32_t block_rank(MgShared& sh, bool flag, uint32_t& total) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t ball = __ballot_sync(0xffffffffu, flag);
+    if (lane == 0) sh.wc[warp] = __popc(ball);
+    __syncthreads();
+    uint32_t off = 0, tot = 0;
+    for (uint32_t w = 0; w < MG_THREADS / 32; w++) {
+        const uint32_t v = sh.wc[w];
+        off += w < warp ? v : 0u;
+        tot += v;
+    }
+    __syncthreads();
+    total = tot;
+    return off + __popc(ball & ((1u << lane) - 1u));
+}
+
+// Level-l cell range of this block (levels >= 1 outside block 0's share).
+__device__ __forceinline__ void block_range(uint32_t C, uint32_t& lo, uint32_t& hi) {
+    lo = (uint32_t)(((uint64_t)C * blockIdx.x) / gridDim.x);
+    hi = (uint32_t)(((uint64_t)C * (blockIdx.x + 1)) / gridDim.x);
+}
+
+// Lists this block's level-0 unknowns (plan order) and level-1 unknowns.
+__device__ void build_lists(Ctx& x) {
+    MgShared& sh = x.sh;
+    const DevParams& P = *x.b.prm;
+    const uint32_t C = P.C, nx = P.nx, ny = P.ny, lo = threadIdx.x & (CHUNK - 1);
+    uint32_t n = 0;
+    for (uint32_t base = 0; base < x.nown; base += MG_THREADS / CHUNK) {
+        const uint32_t e = base + threadIdx.x / CHUNK;
+        uint32_t c = 0, info = 0;
+        if (e < x.nown) {
+            c = x.b.cg_chunk[x.e0 + e] * CHUNK + lo;
+            if (c < C) info = ld_ci(x.b.cinfo, c);
+        }
+        const bool u = info >= (1u << 7);
+        uint32_t tot;
+        const uint32_t pos = n + block_rank(sh, u, tot);
+        if (u && pos < (uint32_t)MG_CELLS) {
+            sh.cell[pos] = c;
+            sh.meta[pos] = (uint16_t)make_meta(info, c, nx, ny);
+        }
+        n += tot;
+    }
+    const MgLevel& l1 = x.m.lv[1];
+    uint32_t n1 = 0, I0, I1;
+    block_range(l1.C, I0, I1);
+    for (uint32_t base = I0; base < I1; base += MG_THREADS) {
+        const uint32_t I = base + threadIdx.x;
+        const bool u = I < I1 && ld_st(l1.st, I).x > 0.0f;
+        uint32_t tot;
+        const uint32_t pos = n1 + block_rank(sh, u, tot);
+        if (u && pos < (uint32_t)MG_L1) sh.l1[pos] = I;
+        n1 += tot;
+    }
+    if (threadIdx.x == 0) {
+        sh.ncell = n;
+        sh.list0 = n <= (uint32_t)MG_CELLS;
+        sh.nl1 = n1;
+        sh.list1 = n1 <= (uint32_t)MG_L1;
+    }
+    __syncthreads();
+}
+
+// f(c, meta) for every level-0 unknown of this block.
 template <class F>
 __device__ __forceinline__ void for_own(const Ctx& x, F f) {
+    const MgShared& sh = x.sh;
+    if (sh.list0) {
+        for (uint32_t e = threadIdx.x; e < sh.ncell; e += MG_THREADS) f(sh.cell[e], (uint32_t)sh.meta[e]);
+        return;
+    }
     const DevParams& P = *x.b.prm;
     const uint32_t C = P.C, lo = threadIdx.x & (CHUNK - 1);
     for (uint32_t e = threadIdx.x / CHUNK; e < x.nown; e += MG_THREADS / CHUNK) {
-        const uint32_t chunk = x.nown <= (uint32_t)MG_KCH ? x.sh.chunk[e] : x.b.cg_chunk[x.e0 + e];
-        const uint32_t c = chunk * CHUNK + lo;
+        const uint32_t c = x.b.cg_chunk[x.e0 + e] * CHUNK + lo;
         if (c >= C) continue;
-        const uint32_t info = x.b.cinfo[c];
-        if (info >= (1u << 7)) f(c, info);  // liquid with a nonzero diagonal
+        const uint32_t info = ld_ci(x.b.cinfo, c);
+        if (info >= (1u << 7)) f(c, make_meta(info, c, P.nx, P.ny));
     }
 }
 
-// Calls f(c, i, j, k, st) for every unknown of coarse level lv, grid-strided.
-template <class F>
-__device__ __forceinline__ void for_level(const MgLevel& lv, F f) {
-    for (uint32_t c = blockIdx.x * MG_THREADS + threadIdx.x; c < lv.C; c += gridDim.x * MG_THREADS) {
-        const float4 sc = lv.st[c];
-        if (sc.x > 0.0f) {
-            const uint32_t i = c % lv.nx, j = (c / lv.nx) % lv.ny, k = c / (lv.nx * lv.ny);
-            f(c, i, j, k, sc);
+// The same cells with loads and stores in two phases: ld(c, meta) (loads
+// only) for MG_BATCH cells of the thread, then st(c, meta, value) for each,
+// so that the batch's loads are in flight together.
+template <int K = MG_BATCH, class Ld, class Stf>
+__device__ __forceinline__ void for_own_batched(const Ctx& x, Ld ld, Stf stf) {
+    const MgShared& sh = x.sh;
+    if (!sh.list0) {
+        for_own(x, [&](uint32_t c, uint32_t meta) { stf(c, meta, ld(c, meta)); });
+        return;
+    }
+    const uint32_t n = sh.ncell;
+    for (uint32_t e = threadIdx.x; e < n; e += K * MG_THREADS) {
+        decltype(ld(0u, 0u)) v[K];
+        uint32_t c[K], mt[K];
+#pragma unroll
+        for (int k = 0; k < K; k++) {
+            const uint32_t ek = e + k * MG_THREADS;
+            if (ek < n) {
+                c[k] = sh.cell[ek];
+                mt[k] = sh.meta[ek];
+                v[k] = ld(c[k], mt[k]);
+            }
         }
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (e + k * MG_THREADS < n) stf(c[k], mt[k], v[k]);
+    }
+}
+
+// f(c, i, j, k, st) for every unknown of coarse level l: level 1 from this
+// block's list, other grid levels over this block's range, local levels
+// (block 0 alone, shared memory) over all cells.
+template <class F>
+__device__ __forceinline__ void for_level(const Ctx& x, uint32_t l, const MgLevel& lv, bool local, F f) {
+    auto visit = [&](uint32_t c, float4 sc) {
+        const uint32_t i = c % lv.nx, j = (c / lv.nx) % lv.ny, k = c / (lv.nx * lv.ny);
+        f(c, i, j, k, sc);
+    };
+    if (local) {
+        for (uint32_t c = threadIdx.x; c < lv.C; c += MG_THREADS) {
+            const float4 sc = ld_st(lv.st, c);
+            if (sc.x > 0.0f) visit(c, sc);
+        }
+        return;
+    }
+    if (l == 1 && x.sh.list1) {
+        for (uint32_t e = threadIdx.x; e < x.sh.nl1; e += MG_THREADS) {
+            const uint32_t c = x.sh.l1[e];
+            visit(c, ld_st(lv.st, c));
+        }
+        return;
+    }
+    uint32_t lo, hi;
+    block_range(lv.C, lo, hi);
+    for (uint32_t c = lo + threadIdx.x; c < hi; c += MG_THREADS) {
+        const float4 sc = ld_st(lv.st, c);
+        if (sc.x > 0.0f) visit(c, sc);
     }
 }
 
 // ---- level 0 passes (b = r, x = z) ----
 
+// pre-smoothing from zero: red z = r/D; black z = (r + sum r_nb/D_nb)/D
 __device__ void pre0(const Ctx& x) {
     const DevParams& P = *x.b.prm;
-    const uint32_t nx = P.nx, ny = P.ny, nxy = nx * ny;
-    const float* r = x.b.r;
+    const uint32_t nx = P.nx, nxy = nx * P.ny;
+    const float* r = x.r;
     const uint16_t* __restrict__ ci = x.b.cinfo;
     float* z = x.m.lv[0].x;
-    for_own(x, [&](uint32_t c, uint32_t info) {
-        const float D = diag0(info);
-        float v = r[c];
-        if (!red_cell(c, nx, ny))
-            v += nbsum0(info, c, nx, nxy, [&](uint32_t n) { return r[n] / diag0(ci[n]); });
-        z[c] = v / D;
+    for_own_batched(
+        x,
+        [&](uint32_t c, uint32_t meta) {
+            float v = r[c];
+            if (meta & META_BLACK)
+                v += nbsum0(meta, c, nx, nxy, [&](uint32_t n, int) { return r[n] / (float)(ld_ci(ci, n) >> 7); });
+            return v / diag0(meta);
+        },
+        [&](uint32_t c, uint32_t, float v) { z[c] = v; });
+}
+
+// The CG update fused with pre0: p += alpha d, r_next = r - alpha q, and the
+// pre-smoothing of r_next (a black cell's red neighbours' r_next computed on
+// the fly from their r and q, which this pass does not change).  Returns this
+// thread's share of r_next . r_next.
+__device__ Df update_pre0(const Ctx& x, float alpha, const float* d, float* r_next) {
+    const DevParams& P = *x.b.prm;
+    const uint32_t nx = P.nx, nxy = nx * P.ny;
+    const float* r = x.r;
+    const float* q = x.b.q;
+    float* p = x.b.p;
+    const uint16_t* __restrict__ ci = x.b.cinfo;
+    float* z = x.m.lv[0].x;
+    Df acc = {0.0f, 0.0f};
+    for_own(x, [&](uint32_t c, uint32_t meta) {
+        const float rn = r[c] - alpha * q[c];
+        float v = rn;
+        if (meta & META_BLACK)
+            v += nbsum0(meta, c, nx, nxy,
+                        [&](uint32_t n, int) { return (r[n] - alpha * q[n]) / (float)(ld_ci(ci, n) >> 7); });
+        p[c] += alpha * d[c];
+        r_next[c] = rn;
+        z[c] = v / diag0(meta);
+        acc = df_add(acc, df_prod(rn, rn));
     });
+    return acc;
+}
+
+// Unknowns of level l (grid pass: this block's share; local: all), eight
+// consecutive lanes per cell: f(I, ii, jj, kk, child d = lane & 7) returns the
+// child's term, the eight terms are summed in a fixed shuffle order and
+// g(I, sum) runs on the first lane.  A cell's children are visited together.
+template <class F, class G>
+__device__ __forceinline__ void for_level8(const Ctx& x, uint32_t l, const MgLevel& lv, bool local, F f, G g) {
+    const uint32_t d = threadIdx.x & 7u, slot = threadIdx.x >> 3;
+    constexpr uint32_t per = MG_THREADS / 8;
+    auto one = [&](bool valid, uint32_t I) {
+        float t = 0.0f;
+        if (valid) {
+            const uint32_t ii = I % lv.nx, jj = (I / lv.nx) % lv.ny, kk = I / (lv.nx * lv.ny);
+            t = f(I, ii, jj, kk, d);
+        }
+        t += __shfl_xor_sync(0xffffffffu, t, 1);
+        t += __shfl_xor_sync(0xffffffffu, t, 2);
+        t += __shfl_xor_sync(0xffffffffu, t, 4);
+        if (valid && d == 0) g(I, t);
+    };
+    if (!local && l == 1 && x.sh.list1) {
+        const uint32_t n = x.sh.nl1;
+        for (uint32_t e0 = 0; e0 < n; e0 += per) {
+            const uint32_t e = e0 + slot;
+            one(e < n, e < n ? x.sh.l1[e] : 0u);
+        }
+        return;
+    }
+    uint32_t lo = 0, hi = lv.C;
+    if (!local) block_range(lv.C, lo, hi);
+    for (uint32_t c0 = lo; c0 < hi; c0 += per) {
+        const uint32_t I = c0 + slot;
+        one(I < hi && ld_st(lv.st, I < hi ? I : lo).x > 0.0f, I);
+    }
 }
 
 // b1 = P^T (r - A z)
 __device__ void restrict0(const Ctx& x) {
     const DevParams& P = *x.b.prm;
     const uint32_t nx = P.nx, ny = P.ny, nz = P.nz, nxy = nx * ny;
-    const float* r = x.b.r;
+    const float* r = x.r;
     const uint16_t* __restrict__ ci = x.b.cinfo;
     const float* z = x.m.lv[0].x;
     const MgLevel& up = x.m.lv[1];
-    for_level(up, [&](uint32_t I, uint32_t ii, uint32_t jj, uint32_t kk, float4) {
-        float s = 0.0f;
-        for (uint32_t d = 0; d < 8; d++) {
+    for_level8(
+        x, 1, up, false,
+        [&](uint32_t, uint32_t ii, uint32_t jj, uint32_t kk, uint32_t d) {
             const uint32_t i = 2 * ii + (d & 1), j = 2 * jj + ((d >> 1) & 1), k = 2 * kk + (d >> 2);
-            if (i >= nx || j >= ny || k >= nz) continue;
+            if (i >= nx || j >= ny || k >= nz) return 0.0f;
             const uint32_t c = i + nx * (j + ny * k);
-            const uint32_t info = ci[c];
-            if (info < (1u << 7)) continue;
-            const float az = diag0(info) * z[c] - nbsum0(info, c, nx, nxy, [&](uint32_t n) { return z[n]; });
-            s += r[c] - az;
-        }
-        up.b[I] = s;
-    });
+            const uint32_t info = ld_ci(ci, c);
+            if (info < (1u << 7)) return 0.0f;
+            return r[c] - (diag0(info) * z[c] - nbsum0(info, c, nx, nxy, [&](uint32_t n, int) { return z[n]; }));
+        },
+        [&](uint32_t I, float s) { up.b[I] = s; });
 }
 
 // correction + black sweep: z_black = (r + sum (z_red + e(parent))) / D
 __device__ void post0_black(const Ctx& x) {
     const DevParams& P = *x.b.prm;
     const uint32_t nx = P.nx, ny = P.ny, nxy = nx * ny;
-    const float* r = x.b.r;
+    const float* r = x.r;
     float* z = x.m.lv[0].x;
     const MgLevel& up = x.m.lv[1];
     const float* e = up.x;
-    for_own(x, [&](uint32_t c, uint32_t info) {
-        if (red_cell(c, nx, ny)) return;
-        const float s = nbsum0(info, c, nx, nxy, [&](uint32_t n) { return z[n] + e[parent_of(n, nx, ny, up)]; });
-        z[c] = (r[c] + s) / diag0(info);
-    });
+    const uint32_t unx = up.nx, unxy = up.nx * up.ny;
+    for_own_batched(
+        x,
+        [&](uint32_t c, uint32_t meta) {
+            if (!(meta & META_BLACK)) return 0.0f;
+            const uint32_t pc = parent_of(c, nx, ny, up);
+            // parent of the neighbour on side s: the own parent, or the next
+            // one when the step leaves the 2x2x2 aggregate
+            auto pn = [&](int side) {
+                switch (side) {
+                    case 0: return (meta & META_IODD) ? pc : pc - 1;
+                    case 1: return (meta & META_IODD) ? pc + 1 : pc;
+                    case 2: return (meta & META_JODD) ? pc : pc - unx;
+                    case 3: return (meta & META_JODD) ? pc + unx : pc;
+                    case 4: return (meta & META_KODD) ? pc : pc - unxy;
+                    default: return (meta & META_KODD) ? pc + unxy : pc;
+                }
+            };
+            const float s = nbsum0(meta, c, nx, nxy, [&](uint32_t n, int side) { return z[n] + e[pn(side)]; });
+            return (r[c] + s) / diag0(meta);
+        },
+        [&](uint32_t c, uint32_t meta, float v) {
+            if (meta & META_BLACK) z[c] = v;
+        });
 }
 
 // red sweep; returns this thread's share of r.z
 __device__ Df post0_red(const Ctx& x) {
     const DevParams& P = *x.b.prm;
-    const uint32_t nx = P.nx, ny = P.ny, nxy = nx * ny;
-    const float* r = x.b.r;
+    const uint32_t nx = P.nx, nxy = nx * P.ny;
+    const float* r = x.r;
     float* z = x.m.lv[0].x;
     Df acc = {0.0f, 0.0f};
-    for_own(x, [&](uint32_t c, uint32_t info) {
-        float zc;
-        const float rc = r[c];
-        if (red_cell(c, nx, ny)) {
-            zc = (rc + nbsum0(info, c, nx, nxy, [&](uint32_t n) { return z[n]; })) / diag0(info);
-            z[c] = zc;
-        } else {
-            zc = z[c];
-        }
-        acc = df_add(acc, df_prod(rc, zc));
-    });
+    for_own_batched(
+        x,
+        [&](uint32_t c, uint32_t meta) {
+            const float rc = r[c];
+            const float zc = (meta & META_BLACK)
+                                 ? z[c]
+                                 : (rc + nbsum0(meta, c, nx, nxy, [&](uint32_t n, int) { return z[n]; })) / diag0(meta);
+            return make_float2(rc, zc);
+        },
+        [&](uint32_t c, uint32_t meta, float2 v) {
+            if (!(meta & META_BLACK)) z[c] = v.y;
+            acc = df_add(acc, df_prod(v.x, v.y));
+        });
     return acc;
 }
 
-// ---- coarse level passes ----
+// ---- coarse level passes (grid levels, or block 0's local levels) ----
 
-__device__ void pre_l(const MgLevel& lv) {
-    const float4* __restrict__ st = lv.st;
-    for_level(lv, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
+__device__ void pre_l(const Ctx& x, uint32_t l, const MgLevel& lv, bool local) {
+    const float4* st = lv.st;
+    for_level(x, l, lv, local, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
         float v = lv.b[c];
         if (((i + j + k) & 1u) != 0u)
-            v += nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.b[n] / st[n].x; });
+            v += nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.b[n] / ld_st(st, n).x; });
         lv.x[c] = v / sc.x;
     });
 }
 
-__device__ void restrict_l(const MgLevel& lv, const MgLevel& up) {
-    const float4* __restrict__ st = lv.st;
-    for_level(up, [&](uint32_t I, uint32_t ii, uint32_t jj, uint32_t kk, float4) {
-        float s = 0.0f;
-        for (uint32_t d = 0; d < 8; d++) {
+__device__ void restrict_l(const Ctx& x, uint32_t l, const MgLevel& lv, const MgLevel& up, bool local) {
+    const float4* st = lv.st;
+    for_level8(
+        x, l + 1, up, local,
+        [&](uint32_t, uint32_t ii, uint32_t jj, uint32_t kk, uint32_t d) {
             const uint32_t i = 2 * ii + (d & 1), j = 2 * jj + ((d >> 1) & 1), k = 2 * kk + (d >> 2);
-            if (i >= lv.nx || j >= lv.ny || k >= lv.nz) continue;
+            if (i >= lv.nx || j >= lv.ny || k >= lv.nz) return 0.0f;
             const uint32_t c = i + lv.nx * (j + lv.ny * k);
-            const float4 sc = st[c];
-            if (!(sc.x > 0.0f)) continue;
-            const float ax = sc.x * lv.x[c] - nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; });
-            s += lv.b[c] - ax;
-        }
-        up.b[I] = s;
-    });
+            const float4 sc = ld_st(st, c);
+            if (!(sc.x > 0.0f)) return 0.0f;
+            return lv.b[c] - (sc.x * lv.x[c] - nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; }));
+        },
+        [&](uint32_t I, float s) { up.b[I] = s; });
 }
 
-__device__ void post_black_l(const MgLevel& lv, const MgLevel& up) {
-    const float4* __restrict__ st = lv.st;
-    for_level(lv, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
+__device__ void post_black_l(const Ctx& x, uint32_t l, const MgLevel& lv, const MgLevel& up, bool local) {
+    const float4* st = lv.st;
+    for_level(x, l, lv, local, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
         if (((i + j + k) & 1u) == 0u) return;
         const float s = nbsum(st, sc, c, i, j, k, lv,
                               [&](uint32_t n) { return lv.x[n] + up.x[parent_of(n, lv.nx, lv.ny, up)]; });
@@ -318,69 +538,98 @@ __device__ void post_black_l(const MgLevel& lv, const MgLevel& up) {
     });
 }
 
-__device__ void post_red_l(const MgLevel& lv) {
-    const float4* __restrict__ st = lv.st;
-    for_level(lv, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
+__device__ void post_red_l(const Ctx& x, uint32_t l, const MgLevel& lv, bool local) {
+    const float4* st = lv.st;
+    for_level(x, l, lv, local, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
         if (((i + j + k) & 1u) != 0u) return;
         lv.x[c] = (lv.b[c] + nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; })) / sc.x;
     });
 }
 
-// Coarsest level: symmetric Gauss-Seidel sweeps from zero in shared memory
-// (block 0 only; the other blocks go on to the next barrier).
-__device__ void coarse_solve(MgShared& sh, const MgLevel& lv) {
-    const uint32_t t = threadIdx.x, C = lv.C, nx = lv.nx, ny = lv.ny, nxy = nx * ny;
-    if (t < C) {
-        sh.cst[t] = lv.st[t];
-        sh.cb[t] = lv.b[t];
-        sh.cx[t] = 0.0f;
-    }
-    __syncthreads();
-    uint32_t i = 0, j = 0, k = 0, col = 0;
-    float4 sc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    if (t < C) {
-        i = t % nx; j = (t / nx) % ny; k = t / nxy;
-        col = (i + j + k) & 1u;
-        sc = sh.cst[t];
-    }
-    for (int h = 0; h < 4 * MG_COARSE_SWEEPS; h++) {
-        // forward sweeps red, black; backward sweeps black, red
-        const uint32_t want = h < 2 * MG_COARSE_SWEEPS ? (uint32_t)(h & 1) : (uint32_t)((h & 1) ^ 1);
-        if (t < C && sc.x > 0.0f && col == want) {
-            float s = 0.0f;
-            if (sc.y != 0.0f) s += sc.y * sh.cx[t + 1];
-            if (sc.z != 0.0f) s += sc.z * sh.cx[t + nx];
-            if (sc.w != 0.0f) s += sc.w * sh.cx[t + nxy];
-            if (i > 0 && sh.cst[t - 1].y != 0.0f) s += sh.cst[t - 1].y * sh.cx[t - 1];
-            if (j > 0 && sh.cst[t - nx].z != 0.0f) s += sh.cst[t - nx].z * sh.cx[t - nx];
-            if (k > 0 && sh.cst[t - nxy].w != 0.0f) s += sh.cst[t - nxy].w * sh.cx[t - nxy];
-            sh.cx[t] = (sh.cb[t] + s) / sc.x;
-        }
-        __syncthreads();
-    }
-    if (t < C) lv.x[t] = sh.cx[t];
+// Block 0's view of level l >= Lg: the global stencil (read-only cache),
+// b and x in shared memory.
+__device__ __forceinline__ MgLevel local_level(const Ctx& x, uint32_t l) {
+    MgLevel v = x.m.lv[l];
+    uint32_t off = 0;
+    for (uint32_t k = x.Lg; k < l; k++) off += x.m.lv[k].C;
+    v.b = x.sh.lb + off;
+    v.x = x.sh.lx + off;
+    return v;
 }
 
-// z = M^-1 r, then the r.z all-reduce (whose barrier ends the cycle).
-__device__ bool vcycle(Ctx& x, Df& rz) {
+// Levels Lg .. L-1 by block 0 alone (block barriers instead of grid
+// barriers): V-cycle with symmetric Gauss-Seidel sweeps from zero on the
+// coarsest level.
+__device__ void local_cycle(const Ctx& x) {
+    const uint32_t L = x.m.L, Lg = x.Lg;
+    {
+        const MgLevel g = x.m.lv[Lg], s = local_level(x, Lg);
+        for (uint32_t c = threadIdx.x; c < g.C; c += MG_THREADS) s.b[c] = g.b[c];
+        __syncthreads();
+    }
+    for (uint32_t l = Lg; l + 1 < L; l++) {
+        const MgLevel lv = local_level(x, l), up = local_level(x, l + 1);
+        pre_l(x, l, lv, true);
+        __syncthreads();
+        restrict_l(x, l, lv, up, true);
+        __syncthreads();
+    }
+    {
+        const MgLevel lv = local_level(x, L - 1);
+        const uint32_t t = threadIdx.x, nx = lv.nx, ny = lv.ny, nxy = nx * ny;
+        uint32_t i = 0, j = 0, k = 0, col = 0;
+        float4 sc = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (t < lv.C) {
+            i = t % nx; j = (t / nx) % ny; k = t / nxy;
+            col = (i + j + k) & 1u;
+            sc = ld_st(lv.st, t);
+            lv.x[t] = 0.0f;
+        }
+        __syncthreads();
+        for (int h = 0; h < 4 * MG_COARSE_SWEEPS; h++) {
+            // forward sweeps red, black; backward sweeps black, red
+            const uint32_t want = h < 2 * MG_COARSE_SWEEPS ? (uint32_t)(h & 1) : (uint32_t)((h & 1) ^ 1);
+            if (t < lv.C && sc.x > 0.0f && col == want)
+                lv.x[t] = (lv.b[t] + nbsum(lv.st, sc, t, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; })) / sc.x;
+            __syncthreads();
+        }
+    }
+    for (uint32_t l = L - 1; l-- > Lg;) {
+        const MgLevel lv = local_level(x, l), up = local_level(x, l + 1);
+        post_black_l(x, l, lv, up, true);
+        __syncthreads();
+        post_red_l(x, l, lv, true);
+        __syncthreads();
+    }
+    {
+        const MgLevel g = x.m.lv[Lg], s = local_level(x, Lg);
+        for (uint32_t c = threadIdx.x; c < g.C; c += MG_THREADS) g.x[c] = s.x[c];
+    }
+}
+
+// z = M^-1 r, then the r.z all-reduce (whose barrier ends the cycle).  With
+// presmoothed, pre0 and its barrier have already run (update_pre0).
+__device__ bool vcycle(Ctx& x, Df& rz, bool presmoothed) {
     const MgBufs& m = x.m;
-    const uint32_t L = m.L;
-    pre0(x);
-    if (!mg_barrier(x)) return false;
-    restrict0(x);
-    if (!mg_barrier(x)) return false;
-    for (uint32_t l = 1; l + 1 < L; l++) {
-        pre_l(m.lv[l]);
-        if (!mg_barrier(x)) return false;
-        restrict_l(m.lv[l], m.lv[l + 1]);
+    const uint32_t Lg = x.Lg;
+    if (!presmoothed) {
+        pre0(x);
         if (!mg_barrier(x)) return false;
     }
-    if (blockIdx.x == 0) coarse_solve(x.sh, m.lv[L - 1]);
+    restrict0(x);
     if (!mg_barrier(x)) return false;
-    for (uint32_t l = L - 2; l >= 1; l--) {
-        post_black_l(m.lv[l], m.lv[l + 1]);
+    for (uint32_t l = 1; l < Lg; l++) {
+        pre_l(x, l, m.lv[l], false);
         if (!mg_barrier(x)) return false;
-        post_red_l(m.lv[l]);
+        restrict_l(x, l, m.lv[l], m.lv[l + 1], false);
+        if (!mg_barrier(x)) return false;
+    }
+    if (blockIdx.x == 0) local_cycle(x);
+    if (!mg_barrier(x)) return false;
+    for (uint32_t l = Lg; l-- > 1;) {
+        post_black_l(x, l, m.lv[l], m.lv[l + 1], false);
+        if (!mg_barrier(x)) return false;
+        post_red_l(x, l, m.lv[l], false);
         if (!mg_barrier(x)) return false;
     }
     post0_black(x);
@@ -392,37 +641,37 @@ __global__ void __launch_bounds__(MG_THREADS, 1) k_mgpcg(DevBufs b, MgBufs m) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     MgShared& sh = *reinterpret_cast<MgShared*>(smem_raw);
     const DevParams& P = *b.prm;
-    const uint32_t G = gridDim.x, tid = threadIdx.x;
+    const uint32_t tid = threadIdx.x;
     const uint32_t* start = b.cg_off + CHUNK + 3;
-    const uint32_t e0 = start[blockIdx.x], e1 = start[blockIdx.x + 1];
-    Ctx x{sh, b, m, e1 - e0, e0, 0u, 0u};
-    if (x.nown <= (uint32_t)MG_KCH)
-        for (uint32_t e = tid; e < x.nown; e += MG_THREADS) sh.chunk[e] = b.cg_chunk[e0 + e];
-    __syncthreads();
-    (void)G;
+    uint32_t Lg = 1;
+    while (Lg + 1 < m.L && m.lv[Lg].C > MG_BLOCK0_CELLS) Lg++;
+    Ctx x{sh, b, m, start[blockIdx.x], start[blockIdx.x + 1] - start[blockIdx.x], Lg, b.r, 0u, 0u};
+    build_lists(x);
     const uint32_t nx = P.nx, nxy = P.nx * P.ny;
     const uint32_t iters = P.iters;
     const bool stop_on = P.tol_sq > 0.0f;
-    float* p = b.p;
-    float* r = b.r;
     float* q = b.q;
     const float* z = m.lv[0].x;
     DevStats* st = b.st;
 
     // r0.r0 (grid_prep left r = rhs - A p0)
     Df acc = {0.0f, 0.0f};
-    for_own(x, [&](uint32_t c, uint32_t) {
-        const float rc = r[c];
-        acc = df_add(acc, df_prod(rc, rc));
-    });
-    Df rs0;
-    if (!mg_allreduce(x, acc, rs0)) return;
-    const double thr = (double)P.tol_sq_d * df_to_double(rs0);
-    Df thr_d;
-    thr_d.hi = (float)thr;
-    thr_d.lo = (float)(thr - (double)thr_d.hi);
-    Df rz, rs = rs0;
-    if (!vcycle(x, rz)) return;
+    for_own_batched(
+        x, [&](uint32_t c, uint32_t) { return x.r[c]; },
+        [&](uint32_t, uint32_t, float rc) { acc = df_add(acc, df_prod(rc, rc)); });
+    Df rs;
+    if (!mg_allreduce(x, acc, rs)) return;
+    if (tid == 0) {
+        const double thr = (double)P.tol_sq_d * df_to_double(rs);
+        const float hi = (float)thr;
+        sh.rs0 = make_float2(rs.hi, rs.lo);
+        sh.thr = make_float2(hi, (float)(thr - (double)hi));
+    }
+    {
+        Df rz;
+        if (!vcycle(x, rz, false)) return;  // its barriers also publish rs0 and thr
+        if (tid == 0) sh.rz = make_float2(rz.hi, rz.lo);
+    }
     float beta = 0.0f;
     uint32_t k = 0;
     for (uint32_t it = 0; it < iters; it++) {
@@ -431,37 +680,40 @@ __global__ void __launch_bounds__(MG_THREADS, 1) k_mgpcg(DevBufs b, MgBufs m) {
         const bool first = it == 0;
         // direction d = z + beta d_prev and q = A d (neighbours' d on the fly)
         acc = Df{0.0f, 0.0f};
-        for_own(x, [&](uint32_t c, uint32_t info) {
-            auto dv = [&](uint32_t n) { return first ? z[n] : z[n] + beta * d_prev[n]; };
-            const float dc = dv(c);
-            const float qc = diag0(info) * dc - nbsum0(info, c, nx, nxy, dv);
-            d_cur[c] = dc;
-            q[c] = qc;
-            acc = df_add(acc, df_prod(dc, qc));
-        });
+        for_own_batched(
+            x,
+            [&](uint32_t c, uint32_t meta) {
+                auto dv = [&](uint32_t n, int) { return first ? z[n] : z[n] + beta * d_prev[n]; };
+                const float dc = dv(c, 0);
+                return make_float2(dc, diag0(meta) * dc - nbsum0(meta, c, nx, nxy, dv));
+            },
+            [&](uint32_t c, uint32_t, float2 v) {
+                d_cur[c] = v.x;
+                q[c] = v.y;
+                acc = df_add(acc, df_prod(v.x, v.y));
+            });
         Df dq;
         if (!mg_allreduce(x, acc, dq)) return;
         // cg_alpha.wgsl:16-22: alpha = 0 when |d.q| <= 1e-30
-        const float alpha = fabsf(dq.hi) > 1e-30f ? df_div(rz, dq) : 0.0f;
-        acc = Df{0.0f, 0.0f};
-        for_own(x, [&](uint32_t c, uint32_t) {
-            p[c] += alpha * d_cur[c];
-            const float rc = r[c] - alpha * q[c];
-            r[c] = rc;
-            acc = df_add(acc, df_prod(rc, rc));
-        });
-        if (!mg_allreduce(x, acc, rs)) return;
+        const float alpha = fabsf(dq.hi) > 1e-30f ? df_div(Df{sh.rz.x, sh.rz.y}, dq) : 0.0f;
+        // residuals alternate between r and r2: neighbours' old values are
+        // read while the new ones are written
+        float* r_next = x.r == b.r ? m.r2 : b.r;
+        if (!mg_allreduce(x, update_pre0(x, alpha, d_cur, r_next), rs)) return;
+        x.r = r_next;
         k = it + 1;
-        if (stop_on && df_le(rs, thr_d)) break;
+        if (stop_on && df_le(rs, Df{sh.thr.x, sh.thr.y})) break;
         if (it + 1 == iters) break;
         Df rz_new;
-        if (!vcycle(x, rz_new)) return;
+        if (!vcycle(x, rz_new, true)) return;
+        const Df rz = {sh.rz.x, sh.rz.y};
         beta = rz.hi > 1e-30f ? df_div(rz_new, rz) : 0.0f;  // cg_beta.wgsl:16-23
-        rz = rz_new;
+        __syncthreads();
+        if (tid == 0) sh.rz = make_float2(rz_new.hi, rz_new.lo);
     }
     if (blockIdx.x == 0 && tid == 0) {
         st->cg_iters = k;
-        st->rs_init = df_to_double(rs0);
+        st->rs_init = df_to_double(Df{sh.rs0.x, sh.rs0.y});
         st->rs_final = df_to_double(rs);
     }
 }

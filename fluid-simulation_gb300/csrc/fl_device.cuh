@@ -323,6 +323,11 @@ FL_HD inline uint32_t mg_levels(uint32_t nx, uint32_t ny, uint32_t nz, uint32_t 
     }
     return L;
 }
+// Relaxation solves from zero (fl_relax.cu): method 0 Jacobi (ping-pong
+// between pa and pb), 1 red-black Gauss-Seidel (in place in pa); *result is
+// the buffer that holds the answer.
+cudaError_t launch_relax(const uint8_t* ct, const float* div, float scale, float* pa, float* pb, uint32_t nx,
+                         uint32_t ny, uint32_t nz, uint32_t method, uint32_t iters, cudaStream_t s, float** result);
 // The CG's plan of active chunks split over G blocks (fl_cg.cu).
 cudaError_t launch_cg_plan(const DevBufs& b, uint32_t G, cudaStream_t s);
 cudaError_t launch_mgpcg(const DevBufs& b, const MgBufs& m, const LaunchCfg& L, cudaStream_t s);

@@ -925,6 +925,49 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     return FL_OK;
 }
 
+fl_status fl_relax_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type, const float* divergence,
+                            float h, float rho, float dt, uint32_t method, uint32_t iters, float* pressure_out) {
+    if (!cell_type || !divergence || !pressure_out) return set_err(nullptr, FL_INVALID_ARG, "NULL argument");
+    if (nx < 3 || ny < 3 || nz < 3 || (uint64_t)nx * ny * nz > (1ull << 30))
+        return set_err(nullptr, FL_INVALID_ARG, "bad grid size");
+    if (!(h > 0.0f) || !(rho > 0.0f) || !(dt > 0.0f)) return set_err(nullptr, FL_INVALID_ARG, "h, rho, dt must be > 0");
+    if (method > 1u) return set_err(nullptr, FL_INVALID_ARG, "method must be FL_RELAX_JACOBI or FL_RELAX_RBGS");
+    fl_status s = device_check(nullptr);
+    if (s != FL_OK) return s;
+    const size_t C = (size_t)nx * ny * nz;
+    const float scale = rho * h * h / dt;  // ProjectionParams::rhs_scale (sim/pressure.rs:31-33)
+    PoolPlan pl;
+    const size_t o_ct = pl.take<uint8_t>(C), o_div = pl.take<float>(C), o_a = pl.take<float>(C),
+                 o_b = pl.take<float>(C);
+    void* pool = nullptr;
+    cudaError_t e = cudaMalloc(&pool, pl.off);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return set_err(nullptr, FL_OOM, "cudaMalloc failed");
+    }
+    char* base = (char*)pool;
+    uint8_t* dct = (uint8_t*)(base + o_ct);
+    float* ddiv = (float*)(base + o_div);
+    float* pa = (float*)(base + o_a);
+    float* pb = (float*)(base + o_b);
+    float* res = pa;
+    cudaStream_t st = nullptr;
+    do {
+        if ((e = cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking)) != cudaSuccess) break;
+        if ((e = cudaMemsetAsync(pool, 0, pl.off, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(dct, cell_type, C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+        if ((e = cudaMemcpyAsync(ddiv, divergence, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
+        if ((e = fl::launch_relax(dct, ddiv, scale, pa, pb, nx, ny, nz, method, iters, st, &res)) != cudaSuccess)
+            break;
+        if ((e = cudaMemcpyAsync(pressure_out, res, 4 * C, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
+        e = cudaStreamSynchronize(st);
+    } while (0);
+    fl_status rs = e != cudaSuccess ? cuda_err(nullptr, e, "fl_relax_pressure") : FL_OK;
+    if (st) cudaStreamDestroy(st);
+    cudaFree(pool);
+    return rs;
+}
+
 fl_status fl_get_particles_device(fl_handle* h, void* dst_dev, uint32_t* ids_dev) {
     if (!h || (!dst_dev && h->n)) return set_err(h, FL_INVALID_ARG, "NULL argument");
     if (h->n) FL_CUDA(h, cudaMemcpyAsync(dst_dev, h->partA, (size_t)h->n * 32, cudaMemcpyDeviceToDevice, h->stream));

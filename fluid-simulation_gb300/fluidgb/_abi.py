@@ -18,6 +18,7 @@ FL_OK, FL_INVALID_ARG, FL_OOM, FL_CUDA_ERROR, FL_NOT_CONVERGED, FL_TIMEOUT, FL_N
 FL_CELL_SOLID, FL_CELL_LIQUID, FL_CELL_AIR = 0, 1, 2
 FL_CG_F32, FL_CG_F64 = 0, 1
 FL_SOLVER_CG, FL_SOLVER_MGPCG = 0, 1
+FL_RELAX_JACOBI, FL_RELAX_RBGS = 0, 1
 
 c_u32 = ctypes.c_uint32
 c_f32 = ctypes.c_float
@@ -119,6 +120,8 @@ SIGNATURES = {
     "fl_solve_pressure": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.POINTER(ctypes.c_uint8), _fp, _fp, _fp,
                                          c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
                                          ctypes.POINTER(FlStats)]),
+    "fl_relax_pressure": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.POINTER(ctypes.c_uint8), _fp, c_f32, c_f32,
+                                         c_f32, c_u32, c_u32, _fp]),
     "fl_solve_pressure_noalloc": (ctypes.c_int, [c_u32, c_u32, c_u32, ctypes.c_void_p, ctypes.c_void_p,
                                                  ctypes.c_void_p, c_f32, c_f32, c_f32, c_u32, c_u32, c_f32, c_u32,
                                                  ctypes.c_void_p, ctypes.POINTER(FlStats)]),
@@ -422,6 +425,19 @@ def solve_pressure(cell_type, div, dims, h, rho, dt, max_iters, warm_start=False
                                       _f32p(pin), _f32p(pout), h, rho, dt, max_iters, 1 if warm_start else 0,
                                       tolerance, precision, ctypes.byref(st)))
     return pout, st.as_dict()
+
+
+def relax_pressure(cell_type, div, dims, h, rho, dt, method, iters, lib=None):
+    """The reference's Jacobi (FL_RELAX_JACOBI) or red-black Gauss-Seidel
+    (FL_RELAX_RBGS) solve from zero on the GPU (fl_relax_pressure)."""
+    lib = lib or load_library()
+    nx, ny, nz = dims
+    ct = np.ascontiguousarray(cell_type, dtype=np.uint8)
+    dv = np.ascontiguousarray(div, dtype=np.float32)
+    pout = np.empty_like(dv)
+    _check(lib, lib.fl_relax_pressure(nx, ny, nz, ct.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), _f32p(dv), h,
+                                      rho, dt, method, iters, _f32p(pout)))
+    return pout
 
 
 class Tape:

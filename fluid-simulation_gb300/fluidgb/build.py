@@ -21,7 +21,7 @@ LIB_NAME = "libfluidgb.so"
 LIB_PATH = os.path.join(OUT_DIR, LIB_NAME)
 
 SOURCES = ["fl_bin.cu", "fl_grid.cu", "fl_cg.cu", "fl_g2p.cu", "fl_adjoint.cu", "fl_host.cpp", "fl_noalloc.cu",
-           "fl_timestep.cpp", "fl_slice.cu", "fl_scene.cu", "fl_mg.cu"]
+           "fl_timestep.cpp", "fl_slice.cu", "fl_scene.cu", "fl_mg.cu", "fl_relax.cu"]
 HEADERS = ["fl_device.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # --fmad=false: no a*b+c contraction anywhere in device code; the parity-critical

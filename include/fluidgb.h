@@ -367,6 +367,18 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
                             float h, float rho, float dt, uint32_t max_iters, uint32_t warm_start,
                             float tolerance, uint32_t cg_precision, fl_stats* stats_out);
 
+/* The reference's relaxation solvers for the same system, from p = 0:
+ * FL_RELAX_JACOBI is jacobi_solve (sim/pressure.rs:68-136), `iters` Jacobi
+ * sweeps; FL_RELAX_RBGS is the red-black Gauss-Seidel sweep of pressure.wgsl,
+ * `iters` times a red phase then a black phase, in place.  scale = rho*h*h/dt
+ * as in ProjectionParams::rhs_scale.  Host arrays of nx*ny*nz cells; the
+ * result is bit-identical to the reference arithmetic (f32). */
+#define FL_RELAX_JACOBI 0u
+#define FL_RELAX_RBGS 1u
+fl_status fl_relax_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type,
+                            const float* divergence, float h, float rho, float dt, uint32_t method, uint32_t iters,
+                            float* pressure_out);
+
 /* Pressure solve that allocates nothing.  No counterpart in the reference:
  * for callers that cannot call cudaMalloc around the solve (a frame loop with
  * a no-allocation rule, a plugin whose host application owns every device

@@ -323,6 +323,33 @@ static void ref_jacobi_iteration(uint32_t nx, uint32_t ny, uint32_t nz, const ui
             }
 }
 
+/* SH/pressure.wgsl:26-61: red-black Gauss-Seidel, in place, from zero;
+ * `iters` times the red phase ((i+j+k)&1 == 0) then the black phase.  The
+ * per-cell update is jacobi_iteration's formula with the neighbours read from
+ * the same buffer; non-liquid cells stay 0. */
+void orc_ref_rbgs_solve(uint32_t nx, uint32_t ny, uint32_t nz, float h, float rho, float dt,
+                        const uint8_t* ct, const float* div, uint32_t iters, float* p_out) {
+    uint32_t C = nx * ny * nz;
+    float scale = rho * h * h / dt;
+    memset(p_out, 0, 4 * (size_t)C);
+    for (uint32_t it = 0; it < iters; it++)
+        for (uint32_t phase = 0; phase < 2; phase++)
+            for (uint32_t k = 0; k < nz; k++)
+                for (uint32_t j = 0; j < ny; j++)
+                    for (uint32_t i = 0; i < nx; i++) {
+                        uint32_t c = i + nx * (j + ny * k);
+                        if (ct[c] != FL_CELL_LIQUID || ((i + j + k) & 1u) != phase) continue;
+                        uint32_t nb[6] = {c - 1, c + 1, c - nx, c + nx, c - nx * ny, c + nx * ny};
+                        float sum = 0.0f, cnt = 0.0f;
+                        for (int s = 0; s < 6; s++) {
+                            if (ct[nb[s]] == FL_CELL_SOLID) continue;
+                            cnt += 1.0f;
+                            if (ct[nb[s]] == FL_CELL_LIQUID) sum += p_out[nb[s]];
+                        }
+                        p_out[c] = cnt > 0.0f ? (sum - scale * div[c]) / cnt : 0.0f;
+                    }
+}
+
 /* S/sim/pressure.rs:120-136 jacobi_solve; ProjectionParams::rhs_scale :31-33 */
 void orc_ref_jacobi_solve(uint32_t nx, uint32_t ny, uint32_t nz, float h, float rho, float dt,
                           const uint8_t* ct, const float* div, uint32_t iters, float* p_out) {

@@ -89,6 +89,9 @@ void orc_ref_fill_wall_zeroed_faces(uint32_t nx, uint32_t ny, uint32_t nz, int a
 /* sim/pressure.rs:43-66 compute_divergence (no drift term). */
 void orc_ref_compute_divergence(uint32_t nx, uint32_t ny, uint32_t nz, float h, const float* u,
                                 const float* v, const float* w, const uint8_t* ct, float* div);
+/* pressure.wgsl:26-61 red-black Gauss-Seidel from zero, `iters` red+black phases. */
+void orc_ref_rbgs_solve(uint32_t nx, uint32_t ny, uint32_t nz, float h, float rho, float dt,
+                        const uint8_t* ct, const float* div, uint32_t iters, float* p_out);
 /* sim/pressure.rs:72-136 jacobi_solve. */
 void orc_ref_jacobi_solve(uint32_t nx, uint32_t ny, uint32_t nz, float h, float rho, float dt,
                           const uint8_t* ct, const float* div, uint32_t iters, float* p_out);

@@ -85,6 +85,8 @@ def load(build=True):
     lib.orc_ref_compute_divergence.argtypes = [_u32, _u32, _u32, ctypes.c_float, _fp, _fp, _fp, _u8p_t, _fp]
     lib.orc_ref_jacobi_solve.argtypes = [_u32, _u32, _u32, ctypes.c_float, ctypes.c_float, ctypes.c_float, _u8p_t,
                                          _fp, _u32, _fp]
+    lib.orc_ref_rbgs_solve.argtypes = [_u32, _u32, _u32, ctypes.c_float, ctypes.c_float, ctypes.c_float, _u8p_t,
+                                       _fp, _u32, _fp]
     lib.orc_ref_apply_poisson.argtypes = [_u32, _u32, _u32, _u8p_t, _fp, _fp]
     lib.orc_ref_cg_solve.restype = _u32
     lib.orc_ref_cg_solve.argtypes = [_u32, _u32, _u32, ctypes.c_float, ctypes.c_float, ctypes.c_float, _u8p_t,
@@ -336,6 +338,14 @@ def ref_jacobi_solve(dims, h, rho, dt, ct, div, iters):
     out = np.empty(dims[0] * dims[1] * dims[2], np.float32)
     lib.orc_ref_jacobi_solve(dims[0], dims[1], dims[2], h, rho, dt, u8p(np.ascontiguousarray(ct, np.uint8)),
                              f32p(np.ascontiguousarray(div, np.float32)), iters, f32p(out))
+    return out
+
+
+def ref_rbgs_solve(dims, h, rho, dt, ct, div, iters):
+    lib = load()
+    out = np.empty(dims[0] * dims[1] * dims[2], np.float32)
+    lib.orc_ref_rbgs_solve(dims[0], dims[1], dims[2], h, rho, dt, u8p(np.ascontiguousarray(ct, np.uint8)),
+                           f32p(np.ascontiguousarray(div, np.float32)), iters, f32p(out))
     return out
 
 

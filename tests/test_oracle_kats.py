@@ -229,6 +229,25 @@ def test_cg_beats_jacobi_16cubed(oracle):  # sim/pressure.rs:615-698
     assert l2_cg <= l2_jac
 
 
+def test_rbgs_restatement_16cubed(oracle):
+    """pressure.wgsl's red-black Gauss-Seidel (no reference test pins it):
+    from zero, its first red phase is the first Jacobi sweep on the red cells
+    (the same update, sim/pressure.rs:72-117, with every neighbour still 0);
+    100 iterations remove more divergence than 200 Jacobi sweeps, as
+    Gauss-Seidel should."""
+    d, ct, u, v, w, div0 = divergent_tank(oracle)
+    k, j, i = np.indices((16, 16, 16))
+    red = (((i + j + k) & 1) == 0).ravel()
+    g1 = oracle.ref_rbgs_solve(d, 1.0, 1.0, 1.0, ct, div0, 1)
+    j1 = oracle.ref_jacobi_solve(d, 1.0, 1.0, 1.0, ct, div0, 1)
+    assert np.array_equal(g1[red], j1[red])
+    assert np.all(g1[ct != 1] == 0.0)
+    l2_before = oracle.ref_l2_divergence(div0, ct)
+    l2_gs = _l2_after(oracle, d, ct, u, v, w, oracle.ref_rbgs_solve(d, 1.0, 1.0, 1.0, ct, div0, 100))
+    l2_jac = _l2_after(oracle, d, ct, u, v, w, oracle.ref_jacobi_solve(d, 1.0, 1.0, 1.0, ct, div0, 200))
+    assert l2_gs < 0.1 * l2_before and l2_gs < l2_jac
+
+
 def test_cg_zero_initial_guess_matches_fixed_iteration_output(oracle):  # sim/pressure.rs:700-721
     d, ct, u, v, w, div = divergent_tank(oracle)
     fixed, _, _, _ = oracle.ref_cg_solve(d, 1.0, 1.0, 1.0, ct, div, 40)

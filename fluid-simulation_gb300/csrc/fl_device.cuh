@@ -108,7 +108,9 @@ struct DevBufs {
 #define FL_HD
 #endif
 FL_HD constexpr size_t cg_plan_words(size_t max_blocks) { return (size_t)CHUNK + 3 + 2 * (max_blocks + 1); }
-FL_HD constexpr size_t cg_x_words(size_t nchunks, size_t max_blocks) { return 8 + 2 * nchunks + 64 * max_blocks; }
+FL_HD constexpr size_t cg_x_words(size_t nchunks, size_t max_blocks) {
+    return 16 + 2 * ((nchunks + 15) & ~(size_t)15) + 64 * max_blocks;
+}
 
 // Buffers of one adjoint step (fl_adjoint.cu).
 struct AdjBufs {

@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--adj-every", type=int, default=10, help="checkpoint interval of that rollout")
     ap.add_argument("--adj-no-plog", action="store_true",
                     help="recompute segments with their pressure solves (default: replay the logged pressure fields)")
+    ap.add_argument("--adj-mgpcg", action="store_true",
+                    help="run the forward+adjoint leg on FL_SOLVER_MGPCG (forward and adjoint solves)")
     ap.add_argument("--adj-cold", action="store_true",
                     help="start every adjoint pressure solve from zero (default: from the next step's solution)")
     return ap.parse_args()
@@ -354,8 +356,12 @@ def run_ours(args):
 
     adj = None
     if args.adj_steps > 0:
-        adj = adjoint_leg(torch, p, parts, args.adj_steps, args.adj_every, spec["iters"], spec["tol"],
+        pa = p.copy()
+        if args.adj_mgpcg:
+            pa.pressure_solver = fluidgb.FL_SOLVER_MGPCG
+        adj = adjoint_leg(torch, pa, parts, args.adj_steps, args.adj_every, spec["iters"], spec["tol"],
                           warm=not args.adj_cold, plog=not args.adj_no_plog)
+        adj["pressure_solver"] = "mgpcg" if args.adj_mgpcg else "cg"
         torch.cuda.set_stream(stream)
 
     # Per-stage device times (CUDA events between stages on the same stream).

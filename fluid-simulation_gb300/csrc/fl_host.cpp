@@ -1072,6 +1072,8 @@ struct fl_tape {
     DevParams hp_cg{};
     fl_stats last{};     // of the last adjoint pressure solve
     bool adj_warm = false;  // start each adjoint solve from the previous lambda
+    fl::MgBufs mg{};        // multigrid hierarchy of the adjoint solve (FL_SOLVER_MGPCG handles)
+    void* mg_pool = nullptr;
 };
 
 extern "C" {
@@ -1155,6 +1157,7 @@ fl_status fl_tape_free(fl_tape* t) {
     if (!t) return FL_OK;
     if (t->h && t->h->stream) cudaStreamSynchronize(t->h->stream);
     if (t->pool) cudaFree(t->pool);
+    if (t->mg_pool) cudaFree(t->mg_pool);
     delete t;
     return FL_OK;
 }
@@ -1293,7 +1296,14 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     FL_CUDA(h, cudaMemsetAsync(cg.st, 0, sizeof(DevStats), st));
     if (t->adj_warm) FL_CUDA(h, fl::launch_adj_thr(a, h->nchunks, t->hp_cg.tol_sq_d, (DevParams*)cg.prm, st));
     FL_CUDA(h, fl::launch_solve_init(cg, h->C, t->rhs, st));
-    FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
+    if (h->prm.pressure_solver == FL_SOLVER_MGPCG) {
+        // the handle's solver: the same system through the multigrid preconditioner
+        fl_status ms = mg_alloc(h, h->nx, h->ny, h->nz, t->cg.r, &t->mg, &t->mg_pool);
+        if (ms != FL_OK) return ms;
+        FL_CUDA(h, fl::launch_mgpcg(cg, t->mg, h->L, st));
+    } else {
+        FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
+    }
     FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));
     for (int ax = 0; ax < 3; ax++) {
         FL_CUDA(h, cudaMemsetAsync(a.wsum[ax], 0, sizeof(float2) * (size_t)h->F3[ax], st));

@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(MG_THREADS, 1) k_mgpcg(DevBufs b, MgBufs m) {
     Df rs;
     if (!mg_allreduce(x, acc, rs)) return;
     if (tid == 0) {
-        const double thr = (double)P.tol_sq_d * df_to_double(rs);
+        const double thr = P.thr_abs ? P.thr_abs_d : (double)P.tol_sq_d * df_to_double(rs);
         const float hi = (float)thr;
         sh.rs0 = make_float2(rs.hi, rs.lo);
         sh.thr = make_float2(hi, (float)(thr - (double)hi));

@@ -210,7 +210,8 @@ fl_status fl_load_state_device(fl_handle* h, const void* src_dev, size_t size);
  * dL_dgrav[3].  Discrete choices (bins, cell types, clamps) are held fixed;
  * the fixed-point P2G normalisation is linearised at its unquantised sums;
  * the pressure solve is differentiated as an exact solve, so the adjoint runs
- * a second CG with the same operator and the handle's cg_precision, to `adj_cg_tol`
+ * a second CG with the same operator and the handle's cg_precision and
+ * pressure_solver (multigrid-preconditioned when the handle's is), to `adj_cg_tol`
  * relative residual or `adj_cg_iters` iterations.  Requires advect_order 1
  * and wall_friction 0.  Gradient buffers are device pointers.
  * fl_tape_last_stats: cg_iterations, rs_initial/rs_final and device_status of

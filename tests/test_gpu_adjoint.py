@@ -235,3 +235,32 @@ def test_adjoint_warm_start_matches_cold_start():
     assert repc < 1e-5 and repw < 1e-5
     assert sum(itw) < sum(itc)
     assert rel < 1e-3 and relg < 1e-3
+
+
+def test_adjoint_through_the_multigrid_solver():
+    """A handle on FL_SOLVER_MGPCG solves its adjoint pressure systems with the
+    multigrid preconditioner too: the gradients agree with the CG handle's to
+    the solves' tolerance, in far fewer adjoint iterations."""
+    torch = pytest.importorskip("torch")
+    from fluidgb import FL_SOLVER_MGPCG
+    from fluidgb.autograd import Rollout
+    p = scenes.params_for(32, iters=400, tol=1e-6, precision=FL_CG_F64, stiffness=0.0)
+    parts = scenes.seed_particles(32, scenes.box(0.5, 0.4), vel_sigma=0.1)
+    n, steps = parts.shape[0], 12
+    g = np.zeros((n, 8), np.float32)
+    g[:, 0:3] = np.random.default_rng(7).standard_normal((n, 3)).astype(np.float32) / n
+    out = []
+    for solver in (0, FL_SOLVER_MGPCG):
+        q = p.copy()
+        q.pressure_solver = solver
+        roll = Rollout(q, n, steps, checkpoint_every=4, adj_cg_iters=400, adj_cg_tol=1e-6)
+        final, ids = roll.forward(parts, (0.0, -9.81, 0.0))
+        g0, gg = roll.backward(torch.from_numpy(g).cuda()[ids])
+        out.append((g0.cpu().numpy().copy(), np.asarray(gg).copy(), sum(roll.adj_cg_iterations)))
+        roll.close()
+    rel = np.linalg.norm(out[1][0] - out[0][0]) / np.linalg.norm(out[0][0])
+    relg = np.linalg.norm(out[1][1] - out[0][1]) / np.linalg.norm(out[0][1])
+    print("adjoint CG vs MGPCG: iterations %d vs %d; gradient rel. difference %.2e (particles), %.2e (gravity)" % (
+        out[0][2], out[1][2], rel, relg))
+    assert out[1][2] * 2 < out[0][2]
+    assert rel < 1e-3 and relg < 1e-3

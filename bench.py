@@ -175,6 +175,16 @@ def cpu_baseline(name, budget_s, seed):
                 k, name, parts.shape[0], spec["n"], threads)}
 
 
+# BASELINE's metric string, shared by both arms.
+METRIC = "FLIP steps/s @128^3 ~2M particles; fwd+adjoint/fwd ratio; CG HBM GB/s"
+
+
+def base_config(workload, spec, n, world):
+    """The workload part of the JSON line's config, identical in both arms."""
+    return {"workload": workload, "grid": [spec["n"]] * 3, "particles": int(n), "cg_max_iters": spec["iters"],
+            "cg_tol": spec["tol"], "flip": 0.95, "dt": "1/120", "parallelism": "replicas" if world > 1 else "single"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -184,12 +194,11 @@ def run_reference(args):
     cb = cpu_baseline(args.workload, budget, scenes.DEFAULT_SEED)
     p, parts, spec = scenes.workload(args.workload)
     line = {
-        "metric": "FLIP steps/s @128^3 ~2M particles",
+        "metric": METRIC,
         "value": cb["value"], "unit": "steps/s", "impl": "reference", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / cb["value"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "grid": [spec["n"]] * 3, "particles": int(parts.shape[0]),
-                   "cg_max_iters": spec["iters"], "cg_tol": spec["tol"], "parallelism": "replicas"},
+        "config": base_config(args.workload, spec, parts.shape[0], world),
         "cpu_baseline": cb,
         "e2e": {"value": cb["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "reference is Rust+WebGPU (no toolchain or graphics stack here); its step is timed as the C "
@@ -417,17 +426,15 @@ def run_ours(args):
 
     if rank == 0:
         line = {
-            "metric": "FLIP steps/s @128^3 ~2M particles; fwd+adjoint/fwd ratio; CG HBM GB/s",
+            "metric": METRIC,
             "value": value, "unit": "steps/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32" if prec == fluidgb.FL_CG_F32 else "f32+f64-reductions",
             "data": "synthetic (seeded dam break, seed 0x5EED + rank)",
-            "config": {"workload": args.workload, "grid": [nx, ny, nz], "particles": n,
-                       "cg_max_iters": spec["iters"], "cg_tol": spec["tol"], "flip": 0.95, "dt": "1/120",
-                       "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "no flush: per-step working set %.0f MB > 129 MB L2" % (
-                           working_set_bytes(n, nx, ny, nz) / 1e6),
-                       "last_cg_iterations": st["cg_iterations"], "liquid_cells": st["liquid_cells"]},
+            "config": dict(base_config(args.workload, spec, n, world),
+                           l2="no flush: per-step working set %.0f MB > 129 MB L2" % (
+                               working_set_bytes(n, nx, ny, nz) / 1e6),
+                           last_cg_iterations=st["cg_iterations"], liquid_cells=st["liquid_cells"]),
             "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": 32 * n,
                     "d2h_bytes_per_step": 32 * n,
                     "path": "fl_step_host: pinned host particles in, 1 substep, particles out, synchronous"},

@@ -76,6 +76,24 @@ def test_invalid_arguments_are_rejected_without_a_device(fluidlib):
     assert fluidlib.fl_create(ctypes.byref(p), 10, ctypes.byref(h)) == 1
     assert fluidlib.fl_step(None, 1) == 1
     assert fluidlib.fl_status_string(5) == b"FL_TIMEOUT"
+    p = scenes.params_for(16)
+    p.pressure_solver = 2               # neither FL_SOLVER_CG nor FL_SOLVER_MGPCG
+    assert fluidlib.fl_create(ctypes.byref(p), 10, ctypes.byref(h)) == 1
+    assert b"pressure_solver" in fluidlib.fl_last_error(None)
+    # relaxation solver: arguments are checked before the device
+    ct = np.zeros(16 ** 3, np.uint8)
+    dv = np.zeros(16 ** 3, np.float32)
+    out = np.zeros(16 ** 3, np.float32)
+    ctp = ct.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+    f32 = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+    assert fluidlib.fl_relax_pressure(16, 16, 16, ctp, f32(dv), 1.0, 1.0, 1.0, 2, 10, f32(out)) == 1  # method
+    assert fluidlib.fl_relax_pressure(16, 16, 16, None, f32(dv), 1.0, 1.0, 1.0, 0, 10, f32(out)) == 1
+    assert fluidlib.fl_relax_pressure(2, 16, 16, ctp, f32(dv), 1.0, 1.0, 1.0, 0, 10, f32(out)) == 1
+    assert fluidlib.fl_relax_pressure(16, 16, 16, ctp, f32(dv), 1.0, 0.0, 1.0, 0, 10, f32(out)) == 1  # rho
+    # tape and replay entry points reject NULL handles
+    assert fluidlib.fl_tape_set_adjoint_warm_start(None, 1) == 1
+    assert fluidlib.fl_copy_pressure_device(None, None) == 1
+    assert fluidlib.fl_step_replay(None, None, None) == 1
 
 
 def test_create_without_gpu_reports_no_device(fluidlib):

@@ -107,3 +107,43 @@ def test_create_without_gpu_reports_no_device(fluidlib):
     h = ctypes.c_void_p()
     assert fluidlib.fl_create(ctypes.byref(p), 10, ctypes.byref(h)) == 6  # FL_NO_DEVICE
     assert not h.value
+
+
+def test_header_compiles_as_c_and_links(fluidlib, tmp_path):
+    """include/fluidgb.h is plain C (a cgo / bindgen consumer sees it that
+    way): a C translation unit using the INTEGRATION example's calls compiles
+    with -std=c99 -Wall -Werror and links against libfluidgb.so."""
+    import shutil
+    import subprocess
+    from fluidgb import _abi
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include "fluidgb.h"
+int main(void) {
+    fl_params p;
+    float origin[3] = {0.0f, 0.0f, 0.0f};
+    fl_handle* h = 0;
+    if (fl_params_default(&p, 32, 32, 32, 1.0f / 32, origin) != FL_OK) return 1;
+    p.pressure_solver = FL_SOLVER_CG;
+    p.cg_precision = FL_CG_F64;
+    if (fl_create(&p, 16, &h) == FL_OK) {
+        fl_step(h, 1);
+        fl_destroy(h);
+    } else {
+        printf("%s\n", fl_last_error(0));
+    }
+    printf("abi %u\n", fl_abi_version());
+    return 0;
+}
+''')
+    exe = tmp_path / "use"
+    lib_dir = os.path.dirname(_abi.LIB_PATH)
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.dirname(HEADER), str(src),
+                        "-L", lib_dir, "-l:" + os.path.basename(_abi.LIB_PATH), "-Wl,-rpath," + lib_dir,
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0 and "abi 1" in out.stdout, out.stdout + out.stderr

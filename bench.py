@@ -56,6 +56,9 @@ def parse():
                     help="recompute segments with their pressure solves (default: replay the logged pressure fields)")
     ap.add_argument("--adj-mgpcg", action="store_true",
                     help="run the forward+adjoint leg on FL_SOLVER_MGPCG (forward and adjoint solves)")
+    ap.add_argument("--adj-solver", choices=["follow", "cg", "mgpcg"], default="mgpcg",
+                    help="solver of the adjoint pressure systems (default: the multigrid-preconditioned CG; "
+                         "the forward keeps the reference CG unless --adj-mgpcg)")
     ap.add_argument("--adj-cold", action="store_true",
                     help="start every adjoint pressure solve from zero (default: from the next step's solution)")
     return ap.parse_args()
@@ -218,7 +221,7 @@ def timed_steps(torch, g, k):
     return e0.elapsed_time(e1)
 
 
-def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol, warm=True, plog=True):
+def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol, warm=True, plog=True, adj_solver=None):
     """Forward+adjoint of a checkpointed rollout against its forward alone.
 
     forward: `steps` substeps from `parts` with a device checkpoint every
@@ -226,15 +229,17 @@ def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol, warm=True, plog
     substep's pressure field; backward: per earlier segment, restore +
     recompute while recording (with `plog`, each substep replayed with its
     logged pressure instead of its CG: the same bits); every step popped through
-    the adjoint (second CG with the forward's iteration cap, tolerance and
-    precision, started from the next step's adjoint pressure unless `warm` is
-    False).  Loss: |centre of mass - (0.7, 0.2, 0.5)|^2.  Timed with CUDA
+    the adjoint (a second solve with the forward's iteration cap, tolerance
+    and precision, by `adj_solver` — None: the handle's — started from the
+    next step's adjoint pressure unless `warm` is False).  Loss: |centre of mass - (0.7, 0.2, 0.5)|^2.  Timed with CUDA
     events on the rollout's stream."""
     from fluidgb.autograd import Rollout
     n = parts.shape[0]
     free0 = torch.cuda.mem_get_info()[0]
+    from fluidgb import FL_SOLVER_FOLLOW
     roll = Rollout(p, n, steps, checkpoint_every=every, adj_cg_iters=cg_iters, adj_cg_tol=cg_tol,
-                   adj_warm_start=warm, pressure_log=plog)
+                   adj_warm_start=warm, pressure_log=plog,
+                   adj_solver=FL_SOLVER_FOLLOW if adj_solver is None else adj_solver)
     parts_d = torch.from_numpy(parts).cuda()
     target = torch.tensor([0.7, 0.2, 0.5], dtype=torch.float64, device="cuda")
     grav = (p.grav[0], p.grav[1], p.grav[2])
@@ -368,9 +373,11 @@ def run_ours(args):
         pa = p.copy()
         if args.adj_mgpcg:
             pa.pressure_solver = fluidgb.FL_SOLVER_MGPCG
+        adj_solver = {"follow": None, "cg": fluidgb.FL_SOLVER_CG, "mgpcg": fluidgb.FL_SOLVER_MGPCG}[args.adj_solver]
         adj = adjoint_leg(torch, pa, parts, args.adj_steps, args.adj_every, spec["iters"], spec["tol"],
-                          warm=not args.adj_cold, plog=not args.adj_no_plog)
+                          warm=not args.adj_cold, plog=not args.adj_no_plog, adj_solver=adj_solver)
         adj["pressure_solver"] = "mgpcg" if args.adj_mgpcg else "cg"
+        adj["adjoint_solver"] = adj["pressure_solver"] if adj_solver is None else args.adj_solver
         torch.cuda.set_stream(stream)
 
     # Per-stage device times (CUDA events between stages on the same stream).

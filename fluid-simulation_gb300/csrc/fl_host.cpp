@@ -1072,8 +1072,9 @@ struct fl_tape {
     DevParams hp_cg{};
     fl_stats last{};     // of the last adjoint pressure solve
     bool adj_warm = false;  // start each adjoint solve from the previous lambda
-    fl::MgBufs mg{};        // multigrid hierarchy of the adjoint solve (FL_SOLVER_MGPCG handles)
+    fl::MgBufs mg{};        // multigrid hierarchy of the adjoint solve (FL_SOLVER_MGPCG)
     void* mg_pool = nullptr;
+    uint32_t adj_solver = 0xffffffffu;  // FL_SOLVER_*, or the handle's pressure_solver
 };
 
 extern "C" {
@@ -1173,6 +1174,14 @@ fl_status fl_tape_set_adjoint_warm_start(fl_tape* t, int enable) {
     fl_handle* h = t->h;
     t->adj_warm = enable != 0;
     FL_CUDA(h, cudaMemsetAsync(t->cg.p, 0, sizeof(float) * (size_t)h->C, h->stream));
+    return FL_OK;
+}
+
+fl_status fl_tape_set_adjoint_solver(fl_tape* t, uint32_t solver) {
+    if (!t) return set_err(nullptr, FL_INVALID_ARG, "tape is NULL");
+    if (solver > FL_SOLVER_MGPCG && solver != FL_SOLVER_FOLLOW)
+        return set_err(t->h, FL_INVALID_ARG, "solver must be FL_SOLVER_CG, FL_SOLVER_MGPCG or FL_SOLVER_FOLLOW");
+    t->adj_solver = solver;
     return FL_OK;
 }
 
@@ -1296,8 +1305,9 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     FL_CUDA(h, cudaMemsetAsync(cg.st, 0, sizeof(DevStats), st));
     if (t->adj_warm) FL_CUDA(h, fl::launch_adj_thr(a, h->nchunks, t->hp_cg.tol_sq_d, (DevParams*)cg.prm, st));
     FL_CUDA(h, fl::launch_solve_init(cg, h->C, t->rhs, st));
-    if (h->prm.pressure_solver == FL_SOLVER_MGPCG) {
-        // the handle's solver: the same system through the multigrid preconditioner
+    const uint32_t solver = t->adj_solver == FL_SOLVER_FOLLOW ? h->prm.pressure_solver : t->adj_solver;
+    if (solver == FL_SOLVER_MGPCG) {
+        // the same system through the multigrid preconditioner
         fl_status ms = mg_alloc(h, h->nx, h->ny, h->nz, t->cg.r, &t->mg, &t->mg_pool);
         if (ms != FL_OK) return ms;
         FL_CUDA(h, fl::launch_mgpcg(cg, t->mg, h->L, st));

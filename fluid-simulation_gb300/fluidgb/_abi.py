@@ -18,6 +18,7 @@ FL_OK, FL_INVALID_ARG, FL_OOM, FL_CUDA_ERROR, FL_NOT_CONVERGED, FL_TIMEOUT, FL_N
 FL_CELL_SOLID, FL_CELL_LIQUID, FL_CELL_AIR = 0, 1, 2
 FL_CG_F32, FL_CG_F64 = 0, 1
 FL_SOLVER_CG, FL_SOLVER_MGPCG = 0, 1
+FL_SOLVER_FOLLOW = 0xFFFFFFFF
 FL_RELAX_JACOBI, FL_RELAX_RBGS = 0, 1
 
 c_u32 = ctypes.c_uint32
@@ -133,6 +134,7 @@ SIGNATURES = {
     "fl_tape_free": (ctypes.c_int, [ctypes.c_void_p]),
     "fl_tape_clear": (ctypes.c_int, [ctypes.c_void_p]),
     "fl_tape_set_adjoint_warm_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "fl_tape_set_adjoint_solver": (ctypes.c_int, [ctypes.c_void_p, c_u32]),
     "fl_tape_count": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32)]),
     "fl_tape_last_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fl_step_record": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -466,6 +468,10 @@ class Tape:
     def set_adjoint_warm_start(self, enable):
         """Start each adjoint solve from the previous one's lambda (resets lambda to zero)."""
         self.fluid._c(self.fluid.lib.fl_tape_set_adjoint_warm_start(self.t, 1 if enable else 0))
+
+    def set_adjoint_solver(self, solver):
+        """FL_SOLVER_CG, FL_SOLVER_MGPCG or FL_SOLVER_FOLLOW (the handle's)."""
+        self.fluid._c(self.fluid.lib.fl_tape_set_adjoint_solver(self.t, solver))
 
     def __len__(self):
         n = c_u32()

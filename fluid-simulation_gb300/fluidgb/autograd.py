@@ -19,7 +19,9 @@ bits, without the solve that dominates the substep.
 Each adjoint pressure solve starts, by default, from the adjoint pressure of
 the step after it (the one solved just before in the backward walk) and stops
 at the cold start's bound |r| <= tol |dL/dp| (fl_tape_set_adjoint_warm_start);
-adj_warm_start=False starts every solve from zero.
+adj_warm_start=False starts every solve from zero.  adj_solver chooses the
+adjoint solves' solver (FL_SOLVER_CG, FL_SOLVER_MGPCG; by default the
+handle's).
 
 Gradients are taken with respect to the initial per-particle state and the
 gravity (body-force) vector, as in the differentiable-rollout workload:
@@ -28,7 +30,7 @@ gravity (body-force) vector, as in the differentiable-rollout workload:
 import numpy as np
 import torch
 
-from ._abi import Fluid
+from ._abi import FL_SOLVER_FOLLOW, Fluid
 
 
 def _as_device_particles(particles, dev):
@@ -47,7 +49,7 @@ class Rollout:
     caller's stream at entry and exit."""
 
     def __init__(self, params, capacity, steps, checkpoint_every=10, adj_cg_iters=1000, adj_cg_tol=1e-6,
-                 adj_warm_start=True, pressure_log=True):
+                 adj_warm_start=True, pressure_log=True, adj_solver=FL_SOLVER_FOLLOW):
         self.dev = torch.device("cuda", torch.cuda.current_device())
         self.stream = torch.cuda.Stream(self.dev)
         self.fluid = Fluid(params, capacity)
@@ -61,6 +63,7 @@ class Rollout:
         self.cells = int(params.gdim[0]) * int(params.gdim[1]) * int(params.gdim[2])
         self.plog = torch.empty((self.steps, self.cells), dtype=torch.float32, device=self.dev) if pressure_log else None
         self.tape = self.fluid.tape(self.k)
+        self.tape.set_adjoint_solver(adj_solver)
         self.checkpoints = {}
         self.taped = None
         self.n = 0

@@ -210,8 +210,8 @@ fl_status fl_load_state_device(fl_handle* h, const void* src_dev, size_t size);
  * dL_dgrav[3].  Discrete choices (bins, cell types, clamps) are held fixed;
  * the fixed-point P2G normalisation is linearised at its unquantised sums;
  * the pressure solve is differentiated as an exact solve, so the adjoint runs
- * a second CG with the same operator and the handle's cg_precision and
- * pressure_solver (multigrid-preconditioned when the handle's is), to `adj_cg_tol`
+ * a second CG with the same operator, the handle's cg_precision and the
+ * tape's adjoint solver (fl_tape_set_adjoint_solver), to `adj_cg_tol`
  * relative residual or `adj_cg_iters` iterations.  Requires advect_order 1
  * and wall_friction 0.  Gradient buffers are device pointers.
  * fl_tape_last_stats: cg_iterations, rs_initial/rs_final and device_status of
@@ -227,6 +227,12 @@ fl_status fl_tape_clear(fl_tape* t);
  * call, on or off, resets the carried adjoint pressure to zero: a backward
  * pass that begins with it does not depend on earlier ones. */
 fl_status fl_tape_set_adjoint_warm_start(fl_tape* t, int enable);
+/* Solver of the adjoint pressure systems: FL_SOLVER_CG, FL_SOLVER_MGPCG, or
+ * FL_SOLVER_FOLLOW (after fl_tape_create) for the handle's pressure_solver.
+ * The adjoint has no reference arithmetic to match, so the multigrid
+ * preconditioner may serve a handle whose forward runs the reference's CG. */
+#define FL_SOLVER_FOLLOW 0xffffffffu
+fl_status fl_tape_set_adjoint_solver(fl_tape* t, uint32_t solver);
 fl_status fl_tape_count(const fl_tape* t, uint32_t* n_out);
 fl_status fl_tape_last_stats(const fl_tape* t, fl_stats* out);
 fl_status fl_step_record(fl_handle* h, fl_tape* t);

@@ -250,17 +250,22 @@ def test_adjoint_through_the_multigrid_solver():
     g = np.zeros((n, 8), np.float32)
     g[:, 0:3] = np.random.default_rng(7).standard_normal((n, 3)).astype(np.float32) / n
     out = []
-    for solver in (0, FL_SOLVER_MGPCG):
+    # (forward solver, adjoint solver): the CG handle, the MGPCG handle, and
+    # the CG handle whose tape solves the adjoint through the preconditioner
+    from fluidgb import FL_SOLVER_CG, FL_SOLVER_FOLLOW
+    for solver, adj in ((0, FL_SOLVER_FOLLOW), (FL_SOLVER_MGPCG, FL_SOLVER_FOLLOW), (0, FL_SOLVER_MGPCG)):
         q = p.copy()
         q.pressure_solver = solver
-        roll = Rollout(q, n, steps, checkpoint_every=4, adj_cg_iters=400, adj_cg_tol=1e-6)
+        roll = Rollout(q, n, steps, checkpoint_every=4, adj_cg_iters=400, adj_cg_tol=1e-6, adj_solver=adj)
         final, ids = roll.forward(parts, (0.0, -9.81, 0.0))
         g0, gg = roll.backward(torch.from_numpy(g).cuda()[ids])
         out.append((g0.cpu().numpy().copy(), np.asarray(gg).copy(), sum(roll.adj_cg_iterations)))
         roll.close()
-    rel = np.linalg.norm(out[1][0] - out[0][0]) / np.linalg.norm(out[0][0])
-    relg = np.linalg.norm(out[1][1] - out[0][1]) / np.linalg.norm(out[0][1])
-    print("adjoint CG vs MGPCG: iterations %d vs %d; gradient rel. difference %.2e (particles), %.2e (gravity)" % (
-        out[0][2], out[1][2], rel, relg))
-    assert out[1][2] * 2 < out[0][2]
-    assert rel < 1e-3 and relg < 1e-3
+    for k, name in ((1, "MGPCG handle"), (2, "CG handle, MGPCG adjoint")):
+        rel = np.linalg.norm(out[k][0] - out[0][0]) / np.linalg.norm(out[0][0])
+        relg = np.linalg.norm(out[k][1] - out[0][1]) / np.linalg.norm(out[0][1])
+        print("adjoint CG vs %s: iterations %d vs %d; gradient rel. difference %.2e (particles), %.2e (gravity)" % (
+            name, out[0][2], out[k][2], rel, relg))
+        assert out[k][2] * 2 < out[0][2]
+        assert rel < 1e-3 and relg < 1e-3
+    assert FL_SOLVER_CG == 0

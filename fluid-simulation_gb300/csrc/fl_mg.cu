@@ -19,19 +19,23 @@
 // the children's diagonals minus twice their internal couplings.  Stored as
 // float4 {diag, weight to +x, +y, +z}; a cell is an unknown when diag > 0.
 // V-cycle: one red-then-black sweep down, black-then-red up, symmetric
-// Gauss-Seidel sweeps on the coarsest level (<= 64 cells, in shared memory of
-// block 0), all from zero: a symmetric positive-definite preconditioner.
+// Gauss-Seidel sweeps on the coarsest level (<= 64 cells), all from zero: a
+// symmetric positive-definite preconditioner.
 //
 // One cooperative persistent kernel per solve, one 1024-thread block per SM.
 // Level-0 cells are owned per block through the CG's plan of active chunks
-// (k_cg_plan); coarser levels are grid-strided.  A pass boundary is a counter
-// barrier (bounded wait, as in k_cg); a dot product is a per-block
-// float-float partial, a barrier and a fixed-order sum, so results repeat
-// bit for bit.  Each smoothing pass computes what it needs of the other
-// colour on the fly (the red values of the pre-smoothing sweep are b/D; the
-// corrected red values of the post-smoothing sweep are x + e(parent)), so a
-// level costs four passes: pre-smooth, residual + restriction, correction +
-// black sweep, red sweep.
+// (k_cg_plan) and listed in shared memory with their stencil masks; level 1's
+// unknowns are listed per block; other grid levels are split into one cell
+// range per block.  The levels of at most MG_BLOCK0_CELLS cells run inside
+// block 0 alone, with block barriers and their b and x in shared memory.  A
+// grid pass boundary is a counter barrier (bounded wait, as in k_cg); a dot
+// product is a per-block float-float partial, a barrier and a fixed-order
+// sum, so results repeat bit for bit.  Each smoothing pass computes what it
+// needs of the other colour on the fly (the red values of the pre-smoothing
+// sweep are b/D; the corrected red values of the post-smoothing sweep are
+// x + e(parent)), so a level costs four passes: pre-smooth, residual +
+// restriction (eight lanes per coarse cell), correction + black sweep, red
+// sweep; on level 0 the CG update is fused with the pre-smoothing.
 #include "fl_device.cuh"
 
 // Vectors written during the solve (r, z, d, the coarse b and x) are read
@@ -49,6 +53,7 @@ constexpr int MG_CELLS = 20480;           // level-0 unknowns listed per block
 constexpr int MG_L1 = 4096;               // level-1 unknowns listed per block
 constexpr int MG_COARSE_SWEEPS = 2;       // symmetric Gauss-Seidel sweeps on the coarsest level
 constexpr int MG_BATCH = 1;               // level-0 cells per thread whose loads are issued together
+                                          // (2 measured slower: register pressure)
 
 // Level-0 cell metadata: bits 0-9 the CG's stencil mask (bit 0 liquid, bit
 // s+1 neighbour s of -x,+x,-y,+y,-z,+z liquid, bits 7-9 the non-solid count),

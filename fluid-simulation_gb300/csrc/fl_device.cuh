@@ -90,6 +90,8 @@ struct DevBufs {
     float* vel[3];
     float* sav[3];
     float *p, *r, *dA, *dB, *q;
+    float* div;            // divergence of the last substep (divergence.wgsl, drift included); 0 off
+                           // liquid cells; null where no one reads it (the stand-alone solves)
     float* part_rr;        // per-chunk f32 tree partials of the initial residual
     float2* chunk_rr_df;   // per-chunk float-float partials {hi, lo} of the initial residual
     uint32_t* cg_chunk;    // CG plan: active chunks grouped by (chunk mod 256), ascending

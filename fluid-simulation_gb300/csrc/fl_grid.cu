@@ -380,6 +380,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
                 const float drift = fminf(__fmul_rn(P.stiff, over), P.drift_clamp);
                 dv = __fsub_rn(dv, drift);
             }
+            if (b.div) b.div[c] = dv;
             // cg_init.wgsl:66-81
             const float rhs = __fmul_rn(-P.scale_rhs, dv);
             float ap = 0.0f;
@@ -400,6 +401,7 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
             b.r[c] = 0.0f;
             b.dA[c] = 0.0f;
             b.cinfo[c] = 0;
+            if (b.div) b.div[c] = 0.0f;
         }
     }
     const int nliq = __syncthreads_count(liquid);

@@ -407,7 +407,7 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
         o_sav[a] = pl.take<float>(h->F3[a]);
     }
     size_t o_p = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C), o_dB = pl.take<float>(C),
-           o_q = pl.take<float>(C);
+           o_q = pl.take<float>(C), o_div = pl.take<float>(C);
     const size_t gmax = (size_t)g_num_sms * g_cg_per_sm;
     size_t o_prr = pl.take<float>(h->nchunks), o_c64 = pl.take<float2>(h->nchunks);
     size_t o_plan = pl.take<uint32_t>(h->nchunks), o_poff = pl.take<uint32_t>(fl::cg_plan_words(gmax));
@@ -467,6 +467,7 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     b.dA = (float*)(base + o_dA);
     b.dB = (float*)(base + o_dB);
     b.q = (float*)(base + o_q);
+    b.div = (float*)(base + o_div);
     b.part_rr = (float*)(base + o_prr);
     b.chunk_rr_df = (float2*)(base + o_c64);
     b.cg_chunk = (uint32_t*)(base + o_plan);
@@ -697,6 +698,12 @@ fl_status fl_get_grid(fl_handle* h, const fl_grid_view* v) {
     if (v->cell_type) FL_CUDA(h, cudaMemcpyAsync(v->cell_type, h->b.ct, C, cudaMemcpyDeviceToHost, h->stream));
     if (v->counts) FL_CUDA(h, cudaMemcpyAsync(v->counts, h->b.counts, 4 * C, cudaMemcpyDeviceToHost, h->stream));
     if (v->offsets) FL_CUDA(h, cudaMemcpyAsync(v->offsets, h->b.offsets, 4 * C, cudaMemcpyDeviceToHost, h->stream));
+    return read_status(h);
+}
+
+fl_status fl_get_divergence(fl_handle* h, float* out) {
+    if (!h || !out) return set_err(h, FL_INVALID_ARG, "NULL argument");
+    FL_CUDA(h, cudaMemcpyAsync(out, h->b.div, sizeof(float) * (size_t)h->C, cudaMemcpyDeviceToHost, h->stream));
     return read_status(h);
 }
 

@@ -113,6 +113,7 @@ SIGNATURES = {
     "fl_apply_impulse": (ctypes.c_int, [ctypes.c_void_p, _fp]),
     "fl_reset": (ctypes.c_int, [ctypes.c_void_p]),
     "fl_get_grid": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlGridView)]),
+    "fl_get_divergence": (ctypes.c_int, [ctypes.c_void_p, _fp]),
     "fl_get_bins": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(c_u32), ctypes.POINTER(c_u32),
                                    ctypes.POINTER(c_u32)]),
     "fl_get_stats": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(FlStats)]),
@@ -341,6 +342,12 @@ class Fluid:
         v.offsets = _u32p(g["offsets"])
         self._c(self.lib.fl_get_grid(self.h, ctypes.byref(v)))
         return g
+
+    def get_divergence(self):
+        """nx*ny*nz float32: the last substep's divergence (0 off liquid cells)."""
+        out = np.empty(self.C, np.float32)
+        self._c(self.lib.fl_get_divergence(self.h, _f32p(out)))
+        return out
 
     def seed(self, blocks, particle_count):
         """generate_particles on the device into this handle; returns the count."""

@@ -173,6 +173,9 @@ fl_status fl_reset(fl_handle* h);
 
 /* Copy grid state of the last substep to host memory. */
 fl_status fl_get_grid(fl_handle* h, const fl_grid_view* view);
+/* Divergence of the last substep's pre-projection velocity, drift term
+ * included (divergence.wgsl:22-59): nx*ny*nz floats, 0 off liquid cells. */
+fl_status fl_get_divergence(fl_handle* h, float* out);
 /* Bins of the last substep's counting sort: per-cell counts and exclusive
  * offsets, and perm[d] = pre-sort slot of the particle placed in slot d.  The
  * permutation is stable (lib.rs:1188-1211).  Any pointer may be NULL. */

@@ -42,6 +42,8 @@ def assert_same_state(g, o, where=""):
             bad = np.flatnonzero(gg[k] != go[k])
             raise AssertionError("%s %s differs at %d entries, first %d: gpu %r oracle %r" % (
                 where, k, bad.size, bad[0], gg[k][bad[0]], go[k][bad[0]]))
+    if not np.array_equal(g.get_divergence(), o.get_divergence()):
+        raise AssertionError("%s divergence differs" % where)
     bg, bo = g.get_bins(), o.get_bins()
     for name, a, b in zip(("counts", "offsets", "perm"), bg, bo):
         assert np.array_equal(a, b), "%s bins.%s" % (where, name)

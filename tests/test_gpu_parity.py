@@ -313,3 +313,18 @@ def test_256_grid_two_steps_bit_exact(lib, oracle):
         assert_same_state(g, o, "256^3 step %d" % s)
     g.close()
     o.close()
+
+
+@pytest.mark.parametrize("workload,steps", [("dam128", 1), ("sphere_pool128", 2), ("block64", 3)])
+def test_configuration_scenes_bit_exact(lib, oracle, workload, steps):
+    """The other configurations' scenes, from their seeded initial states:
+    the full-depth 128^3 dam break (4.19M particles), the sphere falling into
+    the pool, and the 64^3 block with N(0, 0.1^2) initial velocities."""
+    p, parts, _ = scenes.workload(workload)
+    g, o = make_pair(oracle, p, parts)
+    for s in range(steps):
+        g.step(1)
+        o.step(1)
+        assert_same_state(g, o, "%s step %d" % (workload, s))
+    g.close()
+    o.close()

@@ -178,7 +178,7 @@ def cpu_baseline(name, budget_s, seed):
                 k, name, parts.shape[0], spec["n"], threads)}
 
 
-# BASELINE's metric string, shared by both arms.
+# The headline metric (steps/s, forward+adjoint ratio, CG bandwidth), shared by both arms.
 METRIC = "FLIP steps/s @128^3 ~2M particles; fwd+adjoint/fwd ratio; CG HBM GB/s"
 
 

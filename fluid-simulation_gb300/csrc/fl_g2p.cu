@@ -32,6 +32,31 @@ __device__ __forceinline__ void sample(const DevBufs& b, const DevParams& P, int
     const float* __restrict__ fv = b.vel[axis];
     const float* __restrict__ sv = b.sav[axis];
     float fin = 0.0f, sav = 0.0f, wsum = 0.0f;
+    // All eight taps in range and off the static walls (the common case away
+    // from the walls): the same sums in the same order, without the per-tap
+    // tests.
+    const int lo0 = axis == 0 ? 2 : 1, lo1 = axis == 1 ? 2 : 1, lo2 = axis == 2 ? 2 : 1;
+    if (b0 >= lo0 && b0 + 1 <= nx - 2 && b1 >= lo1 && b1 + 1 <= ny - 2 && b2 >= lo2 && b2 + 1 <= nz - 2) {
+#pragma unroll
+        for (int dk = 0; dk < 2; dk++) {
+            const float wz = tent(t2, dk);
+#pragma unroll
+            for (int dj = 0; dj < 2; dj++) {
+                const float wy = tent(t1, dj);
+                const size_t row = (size_t)b0 + (size_t)dim0 * ((size_t)(b1 + dj) + (size_t)dim1 * (b2 + dk));
+#pragma unroll
+                for (int di = 0; di < 2; di++) {
+                    const float w = __fmul_rn(__fmul_rn(tent(t0, di), wy), wz);
+                    fin = __fadd_rn(fin, __fmul_rn(w, __ldg(fv + row + di)));
+                    if (WITH_SAVED) sav = __fadd_rn(sav, __fmul_rn(w, __ldg(sv + row + di)));
+                    wsum = __fadd_rn(wsum, w);
+                }
+            }
+        }
+        out_fin = __fdiv_rn(fin, wsum);
+        out_sav = WITH_SAVED ? __fdiv_rn(sav, wsum) : 0.0f;
+        return;
+    }
 #pragma unroll
     for (int dk = 0; dk < 2; dk++) {
         const int kk = b2 + dk;

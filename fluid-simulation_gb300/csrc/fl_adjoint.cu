@@ -52,6 +52,33 @@ __device__ __forceinline__ void stencil(const DevParams& P, int axis, const floa
         base[b] = __float2int_rz(floorf(g));
         t[b] = g - (float)base[b];
     }
+    // All eight taps in range (and off the static walls when wall_aware): the
+    // same taps in the same order without the per-tap tests.
+    bool all_in = true;
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+        const int lo = wall_aware ? (axis == b ? 2 : 1) : 0;
+        const int hi = wall_aware ? n3[b] - 2 : dim[b] - 1;
+        all_in = all_in && base[b] >= lo && base[b] + 1 <= hi;
+    }
+    if (all_in) {
+#pragma unroll
+        for (int dk = 0; dk < 2; dk++) {
+            const float wz = dk ? t[2] : 1.0f - t[2], sz = dk ? 1.0f : -1.0f;
+#pragma unroll
+            for (int dj = 0; dj < 2; dj++) {
+                const float wy = dj ? t[1] : 1.0f - t[1], sy = dj ? 1.0f : -1.0f;
+                const size_t row = (size_t)base[0] + (size_t)dim[0] * ((size_t)(base[1] + dj) + (size_t)dim[1] * (base[2] + dk));
+#pragma unroll
+                for (int di = 0; di < 2; di++) {
+                    const float wx = di ? t[0] : 1.0f - t[0], sx = di ? 1.0f : -1.0f;
+                    const float dw[3] = {sx * wy * wz, wx * sy * wz, wx * wy * sz};
+                    f(row + di, wx * wy * wz, dw);
+                }
+            }
+        }
+        return;
+    }
 #pragma unroll
     for (int dk = 0; dk < 2; dk++) {
         const int kk = base[2] + dk;

@@ -58,13 +58,13 @@ constexpr uint32_t CHUNK_WEIGHT = 32;
 
 struct CgShared {
     float tree[KT][CHUNK];     // per-chunk products of one pass, tree slot = cell in chunk
-    float vals[VAL_CAP];       // staged partials of one exchange window
+    float vals[VAL_CAP + VAL_CAP / 32];  // staged partials of one exchange window (positions vpos)
     uint32_t cell[CELL_CAP];   // listed liquid cells: bits 0-9 stencil mask, 10-17 cell in chunk, 18-31 chunk
     uint32_t chunk[KCH];       // this block's chunk ids (plan order)
     uint32_t off[CHUNK + 1];   // plan segment offsets
     uint32_t pass_off[MAX_PASS + 1];
     float seg[CHUNK];          // segment sums (cg_reduce_final.wgsl thread accumulators)
-    float red[2 * CG_WARPS];   // float-float warp partials
+    float red[2 * CG_WARPS];   // F64: float-float warp partials; F32: one pass of chunk trees
     uint32_t wcnt[CG_WARPS];
     uint32_t layout, nslot;              // exchange slot layout (0 plan order, 1 lines, 2 one line per block), slots used
     float thr_f;                         // f32 stopping threshold on r.r
@@ -166,6 +166,13 @@ __device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool a
 
 // ---------------------------------------------------------------------------
 // Reductions
+
+// Staging position of entry e of an exchange window: one pad word every 32
+// entries.  Thread li sums its segment's entries in sequence; segments of
+// equal length 16 (a common case) would start on two banks only, so
+// without the pad the segment sums ran 16-way bank conflicted (0.85 vs
+// 0.47 us per exchange at 128^3).
+__device__ __forceinline__ uint32_t vpos(uint32_t e) { return e + (e >> 5); }
 
 // cg_reduce.wgsl:38-49 over s[0..255], evaluated by one warp: lane l forms the
 // level-128 sums of indices l, l+32, l+64, l+96, the level-64 sums of l and
@@ -356,7 +363,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     }
     const uint32_t s0 = bstart[blockIdx.x], s1 = bstart[blockIdx.x + 1];
     const uint32_t m = s1 - s0;  // this block's chunks: plan entries [s0, s1)
-    const uint32_t slot0 = spos[blockIdx.x];  // this block's first slot
     if (tid == 0) sh.nslot = spos[G];
     __syncthreads();
     if (sh.layout != 0u)  // line -> owning block
@@ -445,16 +451,16 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                                 w[k2] = wait_tag(x + v0 + k2 * CG_THREADS, tag, st, acq);
                                 ok = (uint32_t)(w[k2] >> 32) == tag;
                             }
-                            sh.vals[dst[k2]] = __uint_as_float((uint32_t)w[k2]);
+                            sh.vals[vpos(dst[k2])] = __uint_as_float((uint32_t)w[k2]);
                         }
                     }
                 }
             } else if (x) {  // plan order, window [w0, w0 + wn)
                 ok = stage_words(
                     wn, tag, acq, st, sh.vals, [&](uint32_t v) -> const unsigned long long* { return x + w0 + v; },
-                    [&](uint32_t v) -> uint32_t { return v; });
+                    [&](uint32_t v) -> uint32_t { return vpos(v); });
             } else {
-                for (uint32_t i = tid; i < wn; i += CG_THREADS) sh.vals[i] = b.part_rr[plan[w0 + i]];
+                for (uint32_t i = tid; i < wn; i += CG_THREADS) sh.vals[vpos(i)] = b.part_rr[plan[w0 + i]];
             }
             if (__syncthreads_or(!ok)) return false;
             if (tid < (uint32_t)CHUNK) {
@@ -464,11 +470,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 for (; e + 8 <= hi; e += 8) {  // loads first, then the sequential adds
                     float v[8];
 #pragma unroll
-                    for (int k2 = 0; k2 < 8; k2++) v[k2] = sh.vals[e - w0 + k2];
+                    for (int k2 = 0; k2 < 8; k2++) v[k2] = sh.vals[vpos(e - w0 + k2)];
 #pragma unroll
                     for (int k2 = 0; k2 < 8; k2++) acc = __fadd_rn(acc, v[k2]);
                 }
-                for (; e < hi; e++) acc = __fadd_rn(acc, sh.vals[e - w0]);
+                for (; e < hi; e++) acc = __fadd_rn(acc, sh.vals[vpos(e - w0)]);
             }
             if (w0 + wn < A) __syncthreads();
         }
@@ -502,19 +508,29 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         if (warp == 0) {
             Df v = {sh.red[2 * lane], sh.red[2 * lane + 1]};
             v = warp_sum_df(v);
-            if (lane == 0) {
-                publish(words + 16 * blockIdx.x, tag, v.hi, rel);
-                publish(words + 16 * blockIdx.x + 1, tag, v.lo, rel);
-            }
+            // lanes 0 and 1 store {hi, lo} in one instruction (the FP64-reduction
+            // CG stage measured 1.96-1.98 vs 2.10-2.13 ms per substep at 128^3
+            // against two stores by lane 0: readers saw hi before lo)
+            const float lo = __shfl_sync(0xffffffffu, v.lo, 0);
+            if (lane < 2) publish(words + 16 * blockIdx.x + lane, tag, lane ? lo : v.hi, rel);
         }
     };
-    // Warp w publishes the trees of chunks j0 + w and j0 + w + 32 of the pass.
+    // Warp w evaluates the trees of chunks j0 + w and j0 + w + 32 of the pass
+    // into shared memory (sh.red, KT floats); warp 0 then publishes them
+    // together, one store instruction per 32 words, so a polling block finds
+    // a block's slot line complete in one read instead of filling in word by
+    // word (the CG stage measured 2.06 vs 2.21-2.26 ms per substep at 128^3
+    // against one store per tree warp).
+    static_assert(2 * CG_WARPS == KT, "sh.red stages one pass of chunk trees");
     auto publish_trees = [&](uint32_t j0, uint32_t nb, unsigned long long* slots, uint32_t tag, bool rel) {
         __syncthreads();
         for (uint32_t j = warp; j < nb; j += CG_WARPS) {
             const float v = chunk_tree(sh.tree[j], lane);
-            if (lane == 0) publish(slots + slot0 + j0 + j, tag, v, rel);
+            if (lane == 0) sh.red[j] = v;
         }
+        __syncthreads();
+        if (warp == 0)
+            for (uint32_t j = lane; j < nb; j += 32) publish(slots + sh.spos[blockIdx.x] + j0 + j, tag, sh.red[j], rel);
     };
 
     // Initial residual norm (cg_init.wgsl + cg_reduce of r.r).

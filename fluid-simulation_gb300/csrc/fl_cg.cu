@@ -14,14 +14,18 @@
 //   exchange  beta and the convergence test (cg_beta.wgsl); the loop exits.
 //
 // Exchange = grid barrier and reduction in one step.  Every partial is
-// published as one 64-bit word {tag, value} with a release store; each block
-// polls all partials with acquire loads until every word carries the
-// exchange's tag, then reduces them itself.  No counter, no second read of
-// the partials, no broadcast: seeing the tags is the barrier, and all blocks
+// published as one 64-bit word {tag, value}, a block's words stored together
+// by one warp (on the block's own 128-byte lines in the line layouts); each
+// block polls all partials until every word carries the exchange's tag, then
+// reduces them itself.  No counter, no second read of the partials, no
+// broadcast: seeing the tags is the barrier, and all blocks
 // evaluate the same reduction in the same order.  Tags are unique per solve
 // (a per-area epoch advanced by k_cg_plan), so words left by earlier solves
-// never match.  A block's release covers all of its vector writes of the
-// phase, which is what the next phase's neighbour loads need.
+// never match.  Exchange B publishes with release semantics and polls with
+// acquire loads: a block's release covers all of its vector writes of the
+// update phase and the phase before, which is what the next direction +
+// SpMV phase's neighbour loads need.  Exchange A carries only its partials
+// (relaxed).
 //
 // Only 256-cell chunks holding a liquid cell are visited (the rest are zero in
 // every vector).  k_cg_plan lists them once per solve, grouped by residue
@@ -521,16 +525,27 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // a block's slot line complete in one read instead of filling in word by
     // word (the CG stage measured 2.06 vs 2.21-2.26 ms per substep at 128^3
     // against one store per tree warp).
+    // With `rel`, warp 0 issues the release fence (after the barrier that
+    // orders the block's vector writes before it) while warps 1.. evaluate the
+    // trees, and then stores the words relaxed: fence + strong store in one
+    // thread is a release pattern, and the fence's wait for the block's
+    // stores overlaps the trees (1-2 % of the CG stage at 128^3 against a
+    // release store after the trees).
     static_assert(2 * CG_WARPS == KT, "sh.red stages one pass of chunk trees");
     auto publish_trees = [&](uint32_t j0, uint32_t nb, unsigned long long* slots, uint32_t tag, bool rel) {
         __syncthreads();
-        for (uint32_t j = warp; j < nb; j += CG_WARPS) {
-            const float v = chunk_tree(sh.tree[j], lane);
-            if (lane == 0) sh.red[j] = v;
+        if (rel && warp == 0) {
+            asm volatile("fence.acq_rel.gpu;" ::: "memory");
+        } else {
+            const uint32_t w0 = rel ? warp - 1 : warp, nw = rel ? CG_WARPS - 1 : CG_WARPS;
+            for (uint32_t j = w0; j < nb; j += nw) {
+                const float v = chunk_tree(sh.tree[j], lane);
+                if (lane == 0) sh.red[j] = v;
+            }
         }
         __syncthreads();
         if (warp == 0)
-            for (uint32_t j = lane; j < nb; j += 32) publish(slots + sh.spos[blockIdx.x] + j0 + j, tag, sh.red[j], rel);
+            for (uint32_t j = lane; j < nb; j += 32) publish(slots + sh.spos[blockIdx.x] + j0 + j, tag, sh.red[j], false);
     };
 
     // Initial residual norm (cg_init.wgsl + cg_reduce of r.r).

@@ -82,8 +82,11 @@ __device__ __forceinline__ uint32_t make_meta(uint32_t info, uint32_t c, uint32_
 
 __device__ __forceinline__ float diag0(uint32_t meta) { return (float)((meta >> 7) & 7u); }
 
-// Stencils and masks do not change during the solve: read-only cache.
-__device__ __forceinline__ float4 ld_st(const float4* st, uint32_t c) { return __ldg(st + c); }
+// Stencils and masks do not change during the solve: read-only cache; the
+// levels block 0 runs alone read their stencils from its shared-memory copy.
+__device__ __forceinline__ float4 ld_st(const float4* st, uint32_t c) {
+    return __isShared(st) ? st[c] : __ldg(st + c);
+}
 __device__ __forceinline__ uint32_t ld_ci(const uint16_t* ci, uint32_t c) { return __ldg(ci + c); }
 
 // Sum over the liquid neighbours of v(nb, side) (side 0..5 = -x,+x,-y,+y,-z,+z).
@@ -138,6 +141,7 @@ struct Ctx {
     const float* r;     // the current residual (level 0's b)
     uint32_t epoch;     // barrier target
     uint32_t parity;    // exchange slot parity
+    float4* lst;        // block 0: shared-memory copy of the stencils of levels Lg.. (nullptr: global)
 };
 
 __device__ bool mg_barrier(Ctx& x) {
@@ -551,14 +555,15 @@ __device__ void post_red_l(const Ctx& x, uint32_t l, const MgLevel& lv, bool loc
     });
 }
 
-// Block 0's view of level l >= Lg: the global stencil (read-only cache),
-// b and x in shared memory.
+// Block 0's view of level l >= Lg: b, x and (with more than one block) the
+// stencil in shared memory.
 __device__ __forceinline__ MgLevel local_level(const Ctx& x, uint32_t l) {
     MgLevel v = x.m.lv[l];
     uint32_t off = 0;
     for (uint32_t k = x.Lg; k < l; k++) off += x.m.lv[k].C;
     v.b = x.sh.lb + off;
     v.x = x.sh.lx + off;
+    if (x.lst) v.st = x.lst + off;
     return v;
 }
 
@@ -650,8 +655,30 @@ __global__ void __launch_bounds__(MG_THREADS, 1) k_mgpcg(DevBufs b, MgBufs m) {
     const uint32_t* start = b.cg_off + CHUNK + 3;
     uint32_t Lg = 1;
     while (Lg + 1 < m.L && m.lv[Lg].C > MG_BLOCK0_CELLS) Lg++;
-    Ctx x{sh, b, m, start[blockIdx.x], start[blockIdx.x + 1] - start[blockIdx.x], Lg, b.r, 0u, 0u};
+    // With more than one block, block 0 owns no level-0 cells (launch_mgpcg
+    // splits the plan over blocks 1..G-1): it runs the coarse levels alone
+    // while the others wait, and its cell list space holds their stencils, so
+    // its sweeps read shared memory instead of chains of L2 loads.
+    const bool b0_local = gridDim.x > 1;
+    uint32_t e0 = 0, nown = 0;
+    if (!b0_local || blockIdx.x > 0) {
+        const uint32_t pb = b0_local ? blockIdx.x - 1 : 0u;
+        e0 = start[pb];
+        nown = start[pb + 1] - start[pb];
+    }
+    Ctx x{sh, b, m, e0, nown, Lg, b.r, 0u, 0u, nullptr};
     build_lists(x);
+    if (b0_local && blockIdx.x == 0) {
+        static_assert(sizeof(sh.cell) >= MG_LOCAL_TOTAL * sizeof(float4), "local stencils exceed the cell list");
+        float4* lst = reinterpret_cast<float4*>(sh.cell);
+        uint32_t off = 0;
+        for (uint32_t l = Lg; l < m.L; l++) {
+            for (uint32_t c = tid; c < m.lv[l].C; c += MG_THREADS) lst[off + c] = ld_st(m.lv[l].st, c);
+            off += m.lv[l].C;
+        }
+        x.lst = lst;
+        __syncthreads();
+    }
     const uint32_t nx = P.nx, nxy = P.nx * P.ny;
     const uint32_t iters = P.iters;
     const bool stop_on = P.tol_sq > 0.0f;
@@ -785,7 +812,8 @@ int mg_max_blocks_per_sm() {
 // prepared here.  L.cg_blocks blocks (<= MG_PART), at most one per SM.
 cudaError_t launch_mgpcg(const DevBufs& b, const MgBufs& m, const LaunchCfg& L, cudaStream_t s) {
     if (L.cg_blocks < 1 || L.cg_blocks > MG_PART || m.L < 2) return cudaErrorInvalidValue;
-    cudaError_t e = launch_cg_plan(b, (uint32_t)L.cg_blocks, s);
+    // level-0 cells go to blocks 1..G-1 (block 0 runs the coarse levels)
+    cudaError_t e = launch_cg_plan(b, L.cg_blocks > 1 ? (uint32_t)L.cg_blocks - 1 : 1u, s);
     if (e != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(m.bar, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
     const int gb = L.num_sms * 8;

@@ -102,34 +102,39 @@ __device__ __forceinline__ float nbsum0(uint32_t meta, uint32_t c, uint32_t nx, 
     return s;
 }
 
-// Coarse level: sum over the neighbours of w(nb) * v(nb) (a neighbour with a
-// nonzero weight is an unknown).
+// Coarse level: sum over the neighbours of w(nb) * v(nb, i, j, k of nb) (a
+// neighbour with a nonzero weight is an unknown).
 template <class F>
 __device__ __forceinline__ float nbsum(const float4* st, float4 sc, uint32_t c, uint32_t i, uint32_t j, uint32_t k,
                                        const MgLevel& lv, F v) {
     const uint32_t nxy = lv.nx * lv.ny;
     float s = 0.0f;
-    if (sc.y != 0.0f) s += sc.y * v(c + 1);
-    if (sc.z != 0.0f) s += sc.z * v(c + lv.nx);
-    if (sc.w != 0.0f) s += sc.w * v(c + nxy);
+    if (sc.y != 0.0f) s += sc.y * v(c + 1, i + 1, j, k);
+    if (sc.z != 0.0f) s += sc.z * v(c + lv.nx, i, j + 1, k);
+    if (sc.w != 0.0f) s += sc.w * v(c + nxy, i, j, k + 1);
     if (i > 0) {
         const float w = ld_st(st, c - 1).y;
-        if (w != 0.0f) s += w * v(c - 1);
+        if (w != 0.0f) s += w * v(c - 1, i - 1, j, k);
     }
     if (j > 0) {
         const float w = ld_st(st, c - lv.nx).z;
-        if (w != 0.0f) s += w * v(c - lv.nx);
+        if (w != 0.0f) s += w * v(c - lv.nx, i, j - 1, k);
     }
     if (k > 0) {
         const float w = ld_st(st, c - nxy).w;
-        if (w != 0.0f) s += w * v(c - nxy);
+        if (w != 0.0f) s += w * v(c - nxy, i, j, k - 1);
     }
     return s;
 }
+// v(nb) = x[nb], the neighbour's coordinates unused
+#define MG_X_OF(lv) [&](uint32_t n, uint32_t, uint32_t, uint32_t) { return (lv).x[n]; }
 
-__device__ __forceinline__ uint32_t parent_of(uint32_t c, uint32_t nx, uint32_t ny, const MgLevel& up) {
-    const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
+// The coarse cell (aggregate) holding the cell at (i, j, k), or cell c.
+__device__ __forceinline__ uint32_t parent_at(uint32_t i, uint32_t j, uint32_t k, const MgLevel& up) {
     return (i >> 1) + up.nx * ((j >> 1) + up.ny * (k >> 1));
+}
+__device__ __forceinline__ uint32_t parent_of(uint32_t c, uint32_t nx, uint32_t ny, const MgLevel& up) {
+    return parent_at(c % nx, (c / nx) % ny, c / (nx * ny), up);
 }
 
 struct Ctx {
@@ -322,6 +327,25 @@ __device__ __forceinline__ void for_own_batched(const Ctx& x, Ld ld, Stf stf) {
 // f(c, i, j, k, st) for every unknown of coarse level l: level 1 from this
 // block's list, other grid levels over this block's range, local levels
 // (block 0 alone, shared memory) over all cells.
+// (i, j, k) of cell c of a level of at most MG_BLOCK0_CELLS cells by
+// multiply-high with rounded-up reciprocals ceil(2^32 / d): exact because
+// c * d stays below 2^32 (integer division by a runtime divisor is a long
+// instruction sequence, and the levels block 0 runs alone are issue-bound).
+// A divisor of 1 is stored as 0.
+struct SmallDiv {
+    uint32_t nx, nxy, mx, mxy;
+    __device__ __forceinline__ static uint32_t recip(uint32_t d) { return d > 1u ? 0xffffffffu / d + 1u : 0u; }
+    __device__ __forceinline__ explicit SmallDiv(const MgLevel& lv)
+        : nx(lv.nx), nxy(lv.nx * lv.ny), mx(recip(lv.nx)), mxy(recip(lv.nx * lv.ny)) {}
+    __device__ __forceinline__ void ijk(uint32_t c, uint32_t& i, uint32_t& j, uint32_t& k) const {
+        k = mxy ? __umulhi(c, mxy) : c;
+        const uint32_t rem = c - k * nxy;
+        j = mx ? __umulhi(rem, mx) : rem;
+        i = rem - j * nx;
+    }
+};
+static_assert((uint64_t)MG_BLOCK0_CELLS * MG_BLOCK0_CELLS < (1ull << 32), "SmallDiv needs c * divisor < 2^32");
+
 template <class F>
 __device__ __forceinline__ void for_level(const Ctx& x, uint32_t l, const MgLevel& lv, bool local, F f) {
     auto visit = [&](uint32_t c, float4 sc) {
@@ -329,9 +353,14 @@ __device__ __forceinline__ void for_level(const Ctx& x, uint32_t l, const MgLeve
         f(c, i, j, k, sc);
     };
     if (local) {
+        const SmallDiv dv(lv);
         for (uint32_t c = threadIdx.x; c < lv.C; c += MG_THREADS) {
             const float4 sc = ld_st(lv.st, c);
-            if (sc.x > 0.0f) visit(c, sc);
+            if (sc.x > 0.0f) {
+                uint32_t i, j, k;
+                dv.ijk(c, i, j, k);
+                f(c, i, j, k, sc);
+            }
         }
         return;
     }
@@ -405,10 +434,18 @@ template <class F, class G>
 __device__ __forceinline__ void for_level8(const Ctx& x, uint32_t l, const MgLevel& lv, bool local, F f, G g) {
     const uint32_t d = threadIdx.x & 7u, slot = threadIdx.x >> 3;
     constexpr uint32_t per = MG_THREADS / 8;
+    const SmallDiv dv(lv);  // used for local levels only (at most MG_BLOCK0_CELLS cells)
     auto one = [&](bool valid, uint32_t I) {
         float t = 0.0f;
         if (valid) {
-            const uint32_t ii = I % lv.nx, jj = (I / lv.nx) % lv.ny, kk = I / (lv.nx * lv.ny);
+            uint32_t ii, jj, kk;
+            if (local) {
+                dv.ijk(I, ii, jj, kk);
+            } else {
+                ii = I % lv.nx;
+                jj = (I / lv.nx) % lv.ny;
+                kk = I / (lv.nx * lv.ny);
+            }
             t = f(I, ii, jj, kk, d);
         }
         t += __shfl_xor_sync(0xffffffffu, t, 1);
@@ -517,7 +554,8 @@ __device__ void pre_l(const Ctx& x, uint32_t l, const MgLevel& lv, bool local) {
     for_level(x, l, lv, local, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
         float v = lv.b[c];
         if (((i + j + k) & 1u) != 0u)
-            v += nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.b[n] / ld_st(st, n).x; });
+            v += nbsum(st, sc, c, i, j, k, lv,
+                       [&](uint32_t n, uint32_t, uint32_t, uint32_t) { return lv.b[n] / ld_st(st, n).x; });
         lv.x[c] = v / sc.x;
     });
 }
@@ -532,7 +570,7 @@ __device__ void restrict_l(const Ctx& x, uint32_t l, const MgLevel& lv, const Mg
             const uint32_t c = i + lv.nx * (j + lv.ny * k);
             const float4 sc = ld_st(st, c);
             if (!(sc.x > 0.0f)) return 0.0f;
-            return lv.b[c] - (sc.x * lv.x[c] - nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; }));
+            return lv.b[c] - (sc.x * lv.x[c] - nbsum(st, sc, c, i, j, k, lv, MG_X_OF(lv)));
         },
         [&](uint32_t I, float s) { up.b[I] = s; });
 }
@@ -541,8 +579,9 @@ __device__ void post_black_l(const Ctx& x, uint32_t l, const MgLevel& lv, const 
     const float4* st = lv.st;
     for_level(x, l, lv, local, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
         if (((i + j + k) & 1u) == 0u) return;
-        const float s = nbsum(st, sc, c, i, j, k, lv,
-                              [&](uint32_t n) { return lv.x[n] + up.x[parent_of(n, lv.nx, lv.ny, up)]; });
+        const float s = nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n, uint32_t ni, uint32_t nj, uint32_t nk) {
+            return lv.x[n] + up.x[parent_at(ni, nj, nk, up)];
+        });
         lv.x[c] = (lv.b[c] + s) / sc.x;
     });
 }
@@ -551,7 +590,7 @@ __device__ void post_red_l(const Ctx& x, uint32_t l, const MgLevel& lv, bool loc
     const float4* st = lv.st;
     for_level(x, l, lv, local, [&](uint32_t c, uint32_t i, uint32_t j, uint32_t k, float4 sc) {
         if (((i + j + k) & 1u) != 0u) return;
-        lv.x[c] = (lv.b[c] + nbsum(st, sc, c, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; })) / sc.x;
+        lv.x[c] = (lv.b[c] + nbsum(st, sc, c, i, j, k, lv, MG_X_OF(lv))) / sc.x;
     });
 }
 
@@ -600,7 +639,7 @@ __device__ void local_cycle(const Ctx& x) {
             // forward sweeps red, black; backward sweeps black, red
             const uint32_t want = h < 2 * MG_COARSE_SWEEPS ? (uint32_t)(h & 1) : (uint32_t)((h & 1) ^ 1);
             if (t < lv.C && sc.x > 0.0f && col == want)
-                lv.x[t] = (lv.b[t] + nbsum(lv.st, sc, t, i, j, k, lv, [&](uint32_t n) { return lv.x[n]; })) / sc.x;
+                lv.x[t] = (lv.b[t] + nbsum(lv.st, sc, t, i, j, k, lv, MG_X_OF(lv))) / sc.x;
             __syncthreads();
         }
     }

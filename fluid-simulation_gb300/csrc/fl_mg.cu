@@ -153,7 +153,8 @@ __device__ bool mg_barrier(Ctx& x) {
     __syncthreads();
     x.epoch += gridDim.x;
     if (threadIdx.x == 0) {
-        __threadfence();
+        // the release add orders the block's writes (before the barrier
+        // above) ahead of the arrival; a separate fence only added its wait
         red_release_add(x.m.bar, 1u);
         bool ok = true;
         const uint64_t t0 = global_ns();

@@ -50,7 +50,10 @@ def run(p, parts, steps=1):
     return grid, st, x, ids
 
 
-@pytest.mark.parametrize("dims", [(48, 48, 48), (37, 29, 33)])
+# 10^3 runs on one block (it owns the level-0 cells and the coarse levels,
+# stencils read from global memory); 12^3 on two (block 0 the coarse levels
+# with its stencils in shared memory, block 1 every level-0 cell).
+@pytest.mark.parametrize("dims", [(48, 48, 48), (37, 29, 33), (10, 10, 10), (12, 12, 12)])
 def test_mgpcg_residual_against_the_system(oracle, dims):
     nx, ny, nz = dims
     p = scenes.params_for(nx, ny=ny, nz=nz, iters=1000, tol=1e-5, precision=FL_CG_F64, stiffness=0.0,
@@ -73,7 +76,10 @@ def test_mgpcg_residual_against_the_system(oracle, dims):
     res_mg = rel_residual(ct, div, g_mg["pressure"].reshape(nz, ny, nx), scale)
     print("%s: CG %d iterations, |b-Ap|/|b| %.2e; MGPCG %d iterations, %.2e" % (
         dims, s_cg["cg_iterations"], res_cg, s_mg["cg_iterations"], res_mg))
-    assert s_mg["cg_iterations"] * 3 < s_cg["cg_iterations"]
+    if nx >= 32:
+        assert s_mg["cg_iterations"] * 3 < s_cg["cg_iterations"]
+    else:
+        assert s_mg["cg_iterations"] < s_cg["cg_iterations"]
     # both stop on the recurrence residual at 1e-5; the f32 vectors leave the
     # true residual a few times above it
     assert res_cg < 1e-4 and res_mg < 1e-4

@@ -418,8 +418,9 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     cudaError_t e = cudaMalloc(&h->pool, h->pool_bytes);
     if (e != cudaSuccess) {
         (void)cudaGetLastError();
+        const size_t bytes = h->pool_bytes;
         delete h;
-        return set_err(nullptr, FL_OOM, "cudaMalloc of " + std::to_string(h->pool_bytes) + " bytes failed");
+        return set_err(nullptr, FL_OOM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
     }
     char* base = (char*)h->pool;
     if ((e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking)) != cudaSuccess) {

@@ -403,10 +403,21 @@ def run_ours(args):
     achieved = bytes_total / (stage_ms[dom] / 1000.0) / 1e9
     peak, peak_kind = measured_peaks()
     traffic = None
+    traffic_all = {}
     tpath = os.path.join(REPO, "profiles", "traffic.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(args.workload, {}).get(dom)
+            traffic_all = json.load(f).get(args.workload, {})
+        traffic = traffic_all.get(dom)
+    # Every stage against the same byte model and peak (transfer GB/s:
+    # scatter = P2G, g2p = G2P), with ncu's DRAM bytes per launch where captured.
+    stage_roofline = {}
+    for k, ms in stage_ms.items():
+        if ms <= 0.0:
+            continue
+        b = cg_bytes if k == "cg" else algorithmic_bytes(k, n, nx, ny, nz, liquid_avg, iters_avg) * nprof
+        gbs = b / (ms / 1000.0) / 1e9
+        stage_roofline[k] = {"algorithmic_gbs": gbs, "frac": gbs / peak, "traffic": traffic_all.get(k)}
 
     # End to end through the public C ABI with host buffers.
     pin_in = torch.empty((n, 8), dtype=torch.float32, pin_memory=True)
@@ -450,6 +461,7 @@ def run_ours(args):
                          "bytes_model": "cg: 33 B per liquid cell per iteration" if dom == "cg" else dom,
                          "avg_liquid_cells": liquid_avg, "avg_cg_iterations": iters_avg},
             "stage_ms_per_step": {k: v / max(nprof, 1) for k, v in stage_ms.items()},
+            "stage_roofline": stage_roofline,
             "fp64_reductions": fp64,
             "mgpcg": mg,
             "fwd_adjoint": adj,

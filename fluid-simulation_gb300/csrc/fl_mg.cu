@@ -23,11 +23,13 @@
 // symmetric positive-definite preconditioner.
 //
 // One cooperative persistent kernel per solve, one 1024-thread block per SM.
-// Level-0 cells are owned per block through the CG's plan of active chunks
-// (k_cg_plan) and listed in shared memory with their stencil masks; level 1's
-// unknowns are listed per block; other grid levels are split into one cell
-// range per block.  The levels of at most MG_BLOCK0_CELLS cells run inside
-// block 0 alone, with block barriers and their b and x in shared memory.  A
+// Level-0 cells are owned through the CG's plan of active chunks (k_cg_plan,
+// split over blocks 1..G-1 when G > 1) and listed in shared memory with their
+// stencil masks; level 1's unknowns are listed per block; other grid levels
+// are split into one cell range per block.  The levels of at most
+// MG_BLOCK0_CELLS cells run inside block 0 alone, with block barriers and
+// their b, x and stencils in shared memory (the stencils in the cell-list
+// space that block 0 does not need when it owns no level-0 cells).  A
 // grid pass boundary is a counter barrier (bounded wait, as in k_cg); a dot
 // product is a per-block float-float partial, a barrier and a fixed-order
 // sum, so results repeat bit for bit.  Each smoothing pass computes what it

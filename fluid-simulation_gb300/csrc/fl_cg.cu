@@ -114,20 +114,24 @@ __device__ __forceinline__ unsigned long long ld_tag(const unsigned long long* p
     return acq ? ld_acquire_u64(p) : ld_relaxed_u64(p);
 }
 
-// Polls *p until it carries `tag` and returns the word.  Bounded: after about
-// 2 s, or once another block recorded an error, it records FL_TIMEOUT and
-// returns a word without the tag.
-__device__ __noinline__ unsigned long long wait_tag(const unsigned long long* p, uint32_t tag, DevStats* st, bool acq) {
-    const uint64_t t0 = global_ns();
+// Polls *p until it carries `tag` and returns the word.  Bounded: after the
+// settings' wait limit (2 s by default), or once another block recorded an
+// error, it records FL_TIMEOUT and returns a word without the tag.
+__device__ __noinline__ unsigned long long wait_tag(const unsigned long long* p, uint32_t tag, DevStats* st, bool acq,
+                                                    const DevParams* prm) {
+    const uint64_t t0 = global_ns(), limit = wait_limit_ns(prm);
     uint32_t spins = 0;
     unsigned long long w = ld_tag(p, acq);
     while ((uint32_t)(w >> 32) != tag) {
-        if ((++spins & 63u) == 0u) {
-            if (*(volatile uint32_t*)&st->status != 0u) return 0ull;
-            if (global_ns() - t0 > 2000000000ull) {
-                atomicCAS(&st->status, 0u, 5u /* FL_TIMEOUT */);
-                return 0ull;
-            }
+        // The clock is read on the first re-poll and then every 64 polls (so
+        // a limit below one poll's latency expires at the first miss); the
+        // status word, a global load, every 64 polls only.
+        ++spins;
+        const bool slow = (spins & 63u) == 0u;
+        if (slow && *(volatile uint32_t*)&st->status != 0u) return 0ull;
+        if ((slow || spins == 1u) && global_ns() - t0 > limit) {
+            atomicCAS(&st->status, 0u, 5u /* FL_TIMEOUT */);
+            return 0ull;
         }
         w = ld_tag(p, acq);
     }
@@ -141,8 +145,8 @@ __device__ __noinline__ unsigned long long wait_tag(const unsigned long long* p,
 // low; measured faster than re-polling all pending words together).
 // Returns false on abort.
 template <class AddrF, class DstF>
-__device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool acq, DevStats* st, float* vals,
-                                            AddrF addr, DstF dst) {
+__device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool acq, DevStats* st,
+                                            const DevParams* prm, float* vals, AddrF addr, DstF dst) {
     bool ok = true;
     for (uint32_t v0 = threadIdx.x; v0 < nvirt; v0 += STAGE_BATCH * CG_THREADS) {
         unsigned long long w[STAGE_BATCH];
@@ -158,7 +162,7 @@ __device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool a
             const unsigned long long* a = v < nvirt ? addr(v) : nullptr;
             if (a && ok) {
                 if ((uint32_t)(w[k] >> 32) != tag) {
-                    w[k] = wait_tag(a, tag, st, acq);
+                    w[k] = wait_tag(a, tag, st, acq, prm);
                     ok = (uint32_t)(w[k] >> 32) == tag;
                 }
                 vals[dst(v)] = __uint_as_float((uint32_t)w[k]);
@@ -452,7 +456,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                     for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
                         if (dst[k2] != 0xffffffffu && ok) {
                             if ((uint32_t)(w[k2] >> 32) != tag) {
-                                w[k2] = wait_tag(x + v0 + k2 * CG_THREADS, tag, st, acq);
+                                w[k2] = wait_tag(x + v0 + k2 * CG_THREADS, tag, st, acq, b.prm);
                                 ok = (uint32_t)(w[k2] >> 32) == tag;
                             }
                             sh.vals[vpos(dst[k2])] = __uint_as_float((uint32_t)w[k2]);
@@ -461,7 +465,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 }
             } else if (x) {  // plan order, window [w0, w0 + wn)
                 ok = stage_words(
-                    wn, tag, acq, st, sh.vals, [&](uint32_t v) -> const unsigned long long* { return x + w0 + v; },
+                    wn, tag, acq, st, b.prm, sh.vals, [&](uint32_t v) -> const unsigned long long* { return x + w0 + v; },
                     [&](uint32_t v) -> uint32_t { return vpos(v); });
             } else {
                 for (uint32_t i = tid; i < wn; i += CG_THREADS) sh.vals[vpos(i)] = b.part_rr[plan[w0 + i]];
@@ -492,7 +496,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // over blocks, then a shuffle tree), so no broadcast is needed.
     auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, Df& out) -> bool {
         const bool ok = stage_words(
-            2 * G, tag, acq, st, sh.vals,
+            2 * G, tag, acq, st, b.prm, sh.vals,
             [&](uint32_t v) -> const unsigned long long* { return words + (v >> 1) * 16u + (v & 1u); },
             [&](uint32_t v) -> uint32_t { return v; });
         if (__syncthreads_or(!ok)) return false;

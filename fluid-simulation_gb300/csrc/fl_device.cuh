@@ -44,6 +44,10 @@ struct DevParams {
     double thr_abs_d;
     float thr_abs_f;
     uint32_t thr_abs;
+    // Bound on every device-side wait (CG exchange polls, multigrid barrier)
+    // in ns; 0 = the default of 2 s.  On expiry the kernel records FL_TIMEOUT
+    // and every block returns.
+    uint64_t wait_ns;
 };
 
 // Per-step device counters and results.
@@ -244,6 +248,10 @@ __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
+}
+__device__ __forceinline__ uint64_t wait_limit_ns(const DevParams* P) {
+    const uint64_t w = P->wait_ns;
+    return w ? w : 2000000000ull;
 }
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
     uint32_t v;

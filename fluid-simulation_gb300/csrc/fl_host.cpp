@@ -53,6 +53,7 @@ struct fl_handle {
     float4* slice_buf = nullptr;  // device staging of fl_grid_slice (nx*ny float4), allocated on first use
     fl::MgBufs mg{};              // MGPCG hierarchy, allocated when that solver is first selected
     void* mg_pool = nullptr;
+    uint64_t wait_ns = 0;         // device-side wait limit (fl_set_wait_timeout; 0 = default)
     std::string err;
 };
 
@@ -71,6 +72,14 @@ fl_status set_err(fl_handle* h, fl_status s, const std::string& msg) {
 fl_status cuda_err(fl_handle* h, cudaError_t e, const char* what) {
     return set_err(h, FL_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
 }
+
+}  // namespace
+
+// The message slot fl_last_error(NULL) reads, for entry points in other
+// translation units (fl_noalloc.cu).
+void fl_record_global_error(const std::string& msg) { g_err = msg; }
+
+namespace {
 
 #define FL_CUDA(h, call)                                        \
     do {                                                        \
@@ -273,6 +282,7 @@ cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEve
 
 fl_status upload_params(fl_handle* h) {
     derive(h->prm, h->n, h->hp);
+    h->hp.wait_ns = h->wait_ns;
     FL_CUDA(h, cudaMemcpyAsync(h->dprm, &h->hp, sizeof(DevParams), cudaMemcpyHostToDevice, h->stream));
     return FL_OK;
 }
@@ -663,6 +673,12 @@ fl_status fl_set_stream(fl_handle* h, void* cuda_stream) {
     FL_CUDA(h, cudaStreamSynchronize(h->stream));
     h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
     return FL_OK;
+}
+
+fl_status fl_set_wait_timeout(fl_handle* h, uint64_t ns) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    h->wait_ns = ns;
+    return upload_params(h);
 }
 
 fl_status fl_apply_impulse(fl_handle* h, const float dv[3]) {
@@ -1307,6 +1323,7 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     q.cg_precision = h->prm.cg_precision;
     derive(q, h->n, t->hp_cg);
     t->hp_cg.scale_rhs = -1.0f;
+    t->hp_cg.wait_ns = h->wait_ns;
     DevBufs cg = t->cg;
     cg.ct = const_cast<uint8_t*>(a.ct);
     FL_CUDA(h, cudaMemcpyAsync((void*)cg.prm, &t->hp_cg, sizeof(DevParams), cudaMemcpyHostToDevice, st));

@@ -159,19 +159,20 @@ __device__ bool mg_barrier(Ctx& x) {
         // above) ahead of the arrival; a separate fence only added its wait
         red_release_add(x.m.bar, 1u);
         bool ok = true;
-        const uint64_t t0 = global_ns();
+        const uint64_t t0 = global_ns(), limit = wait_limit_ns(x.b.prm);
         uint32_t spins = 0;
         while (ld_acquire(x.m.bar) < x.epoch) {
-            if ((++spins & 63u) == 0u) {
-                if (*(volatile uint32_t*)&x.b.st->status != 0u) {
-                    ok = false;
-                    break;
-                }
-                if (global_ns() - t0 > 2000000000ull) {
-                    atomicCAS(&x.b.st->status, 0u, 5u /* FL_TIMEOUT */);
-                    ok = false;
-                    break;
-                }
+            // clock on the first re-poll and every 64 polls, status every 64
+            ++spins;
+            const bool slow = (spins & 63u) == 0u;
+            if (slow && *(volatile uint32_t*)&x.b.st->status != 0u) {
+                ok = false;
+                break;
+            }
+            if ((slow || spins == 1u) && global_ns() - t0 > limit) {
+                atomicCAS(&x.b.st->status, 0u, 5u /* FL_TIMEOUT */);
+                ok = false;
+                break;
             }
         }
         x.sh.ok = ok;

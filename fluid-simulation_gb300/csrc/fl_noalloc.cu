@@ -21,8 +21,10 @@
 //
 // In host code `g_noalloc_scratch` is a host-side stand-in, not a device
 // address.  The device address is obtained once per device, with that device
-// current, by cudaGetSymbolAddress on the first call on that device; that
-// first call should therefore happen before any stream capture.
+// current, by cudaGetSymbolAddress on the first call on that device.  Every
+// call copies the solve's statistics back and synchronizes the caller's
+// stream, so the entry point cannot be called while that stream is being
+// captured into a CUDA graph.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -32,6 +34,8 @@
 
 #include "../../include/fluidgb.h"
 #include "fl_device.cuh"
+
+void fl_record_global_error(const std::string& msg);  // fl_host.cpp
 
 namespace {
 
@@ -68,11 +72,17 @@ std::mutex g_mu;
 void* g_scratch_dev[kMaxDevices] = {};
 int g_sms[kMaxDevices] = {};
 int g_cg_per_sm[kMaxDevices] = {};
-// The entry point reports failures through its fl_status alone (it is the one
-// addition to the ABI and has no error-string getter); `m` documents the case.
+// Failures return their fl_status and leave the message where
+// fl_last_error(NULL) reads it (the slot fl_solve_pressure uses).
 fl_status fail(fl_status s, const std::string& m) {
-    (void)m;
+    fl_record_global_error("fl_solve_pressure_noalloc: " + m);
     return s;
+}
+
+// True when byte ranges [a, a + na) and [b, b + nb) share a byte.
+bool overlaps(const void* a, size_t na, const void* b, size_t nb) {
+    const uintptr_t x = (uintptr_t)a, y = (uintptr_t)b;
+    return x < y + nb && y < x + na;
 }
 
 // Writes the settings block and clears the counters the CG relies on.
@@ -121,6 +131,11 @@ extern "C" fl_status fl_solve_pressure_noalloc(uint32_t nx, uint32_t ny, uint32_
         return fail(FL_INVALID_ARG, "grid of " + std::to_string(cells) + " cells exceeds the no-allocation limit of " +
                                         std::to_string((unsigned long long)FL_NOALLOC_MAX_CELLS) +
                                         " cells; use fl_solve_pressure");
+    // The warm-start residual reads neighbouring pressures while other threads
+    // overwrite pressure; the solve reads divergence and cell types throughout.
+    if (overlaps(pressure_dev, 4 * cells, divergence_dev, 4 * cells) ||
+        overlaps(pressure_dev, 4 * cells, cell_type_dev, cells))
+        return fail(FL_INVALID_ARG, "pressure_dev must not overlap divergence_dev or cell_type_dev");
     if (!(h > 0.0f) || !(rho > 0.0f) || !(dt > 0.0f)) return fail(FL_INVALID_ARG, "h, rho, dt must be > 0");
     if (cg_precision > 1u) return fail(FL_INVALID_ARG, "cg_precision must be FL_CG_F32 or FL_CG_F64");
     int dev = 0;

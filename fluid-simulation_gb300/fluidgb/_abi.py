@@ -105,6 +105,7 @@ SIGNATURES = {
     "fl_step_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, c_u32]),
     "fl_step_host": (ctypes.c_int, [ctypes.c_void_p, _fp, _fp, c_u32, c_u32]),
     "fl_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_set_wait_timeout": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "fl_set_profiling": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "fl_get_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),
@@ -317,6 +318,10 @@ class Fluid:
 
     def set_stream(self, stream_ptr):
         self._c(self.lib.fl_set_stream(self.h, ctypes.c_void_p(stream_ptr)))
+
+    def set_wait_timeout(self, ns):
+        """Limit of the device-side waits in ns (0 = the default 2 s)."""
+        self._c(self.lib.fl_set_wait_timeout(self.h, int(ns)))
 
     def apply_impulse(self, dv):
         v = (ctypes.c_float * 3)(*dv)

@@ -161,7 +161,18 @@ fl_status fl_step_device(fl_handle* h, void* particles_dev, uint32_t n);
  * pressure; particle ids are not maintained by this call.  n <= capacity. */
 fl_status fl_step_host(fl_handle* h, const float* in, float* out, uint32_t n, uint32_t substeps);
 
+/* Wait for the handle's stream; returns FL_TIMEOUT (and clears it) when a
+ * device-side wait of an earlier substep expired.  Replaces the device-lost
+ * status word the reference polls (gpu/mod.rs:245-250). */
 fl_status fl_sync(fl_handle* h);
+/* Limit of every device-side wait of this handle's kernels (the CG exchange
+ * polls and the multigrid barrier), in nanoseconds; 0 = the default of 2 s.
+ * When a wait runs out, the solve records FL_TIMEOUT and every block returns;
+ * the substep finishes with the pressure the solve had reached, the next
+ * fl_sync / fl_step_host / read-back reports FL_TIMEOUT, and the handle stays
+ * usable.  Applies from the next enqueued substep.  No counterpart in the
+ * reference (a WebGPU device has no such watchdog). */
+fl_status fl_set_wait_timeout(fl_handle* h, uint64_t ns);
 /* Use a caller stream (cudaStream_t passed as void*; NULL = the handle's own). */
 fl_status fl_set_stream(fl_handle* h, void* cuda_stream);
 
@@ -396,13 +407,16 @@ fl_status fl_relax_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
  * start-up).  Same solve and settings as fl_solve_pressure, but inputs and
  * output are DEVICE pointers: cell types (u8), divergence, and pressure
  * (read as the initial guess when warm_start != 0, overwritten with the
- * result).  The CG scratch is one static device array sized for
- * FL_NOALLOC_MAX_CELLS cells (about 4.6 MB, held by every GPU that loads the
- * library until exit); larger grids return FL_INVALID_ARG.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress), so make
- * it before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race.  Enqueues on `cuda_stream` (NULL = default stream) and
- * waits for it; fills stats_out if non-NULL.  No error string is recorded. */
+ * result); pressure must not overlap the other two (FL_INVALID_ARG).  The CG
+ * scratch is one static device array sized for FL_NOALLOC_MAX_CELLS cells
+ * (about 4.6 MB, held by every GPU that loads the library until exit); larger
+ * grids return FL_INVALID_ARG.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress).  All calls share the array:
+ * calls that overlap on the GPU race.  Enqueues on `cuda_stream` (NULL =
+ * default stream), copies the statistics back and synchronizes that stream,
+ * so it cannot be called while the stream is being captured into a graph;
+ * fills stats_out if non-NULL.  A failure leaves its message in
+ * fl_last_error(NULL). */
 #define FL_NOALLOC_MAX_CELLS 262144u
 fl_status fl_solve_pressure_noalloc(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t* cell_type_dev,
                                     const float* divergence_dev, float* pressure_dev, float h, float rho,

@@ -328,3 +328,60 @@ def test_configuration_scenes_bit_exact(lib, oracle, workload, steps):
         assert_same_state(g, o, "%s step %d" % (workload, s))
     g.close()
     o.close()
+
+
+def test_128_grid_thirty_steps_bit_exact(lib, oracle):
+    """The benchmarked configuration (128^3, 2,000,376 particles, CG <= 200 at
+    1e-5) over 30 substeps: every substep of the first five, then every fifth,
+    compared with the oracle by value equality (fluid.rs:1436-1715 per substep)."""
+    p, parts, _ = scenes.workload("dam128_2m")
+    g, o = make_pair(oracle, p, parts)
+    done = 0
+    for k in (1, 2, 3, 4, 5, 10, 15, 20, 25, 30):
+        g.step(k - done)
+        o.step(k - done)
+        done = k
+        assert_same_state(g, o, "128^3 after %d steps" % k)
+    g.close()
+    o.close()
+
+
+def test_128_grid_fp64_reductions_track_the_oracle(lib, oracle):
+    """FL_CG_F64 on the benchmarked configuration, 20 substeps.  Before every
+    substep the oracle (the reference step with double inner products) takes
+    the GPU's particles and warm-start pressure, and both take the step; the
+    float-float reductions then agree with the double ones to 1e-5 relative in
+    face velocity and pressure, 1e-6 in position, and in the iteration count
+    to within one."""
+    p, parts, _ = scenes.workload("dam128_2m", precision=FL_CG_F64)
+    n = parts.shape[0]
+    g = Fluid(p, n)
+    g.set_particles(parts)
+    o = oracle.OracleFluid(p, n)
+    worst = {"velocity": 0.0, "pressure": 0.0, "position": 0.0}
+    for s in range(20):
+        x_in, id_in = g.get_particles()
+        p_in = g.get_grid()["pressure"]
+        g.step(1)
+        o.set_particles(x_in)
+        o.set_pressure(p_in)
+        o.step(1)
+        gg, og = g.get_grid(), o.get_grid()
+        vscale = max(max(np.abs(og[k]).max() for k in ("u", "v", "w")), 1e-30)
+        dv = max(np.abs(gg[k].astype(np.float64) - og[k]).max() for k in ("u", "v", "w")) / vscale
+        pscale = max(np.abs(og["pressure"]).max(), 1e-30)
+        dp = np.abs(gg["pressure"].astype(np.float64) - og["pressure"]).max() / pscale
+        xg, ig = g.get_particles()
+        xo, io = o.get_particles()
+        assert np.array_equal(ig, id_in[io]), "step %d: bin order" % s
+        dx = np.abs(xg[:, 0:3].astype(np.float64) - xo[:, 0:3]).max()
+        worst["velocity"] = max(worst["velocity"], dv)
+        worst["pressure"] = max(worst["pressure"], dp)
+        worst["position"] = max(worst["position"], dx)
+        assert dv <= 1e-5 and dp <= 1e-5 and dx <= 1e-6, (s, dv, dp, dx)
+        assert abs(g.stats()["cg_iterations"] - o.stats()["cg_iterations"]) <= 1, s
+        assert g.stats()["device_status"] == 0
+    print("FL_CG_F64 vs oracle over 20 substeps of dam128_2m: max rel velocity %.2e, pressure %.2e, "
+          "max abs position %.2e" % (worst["velocity"], worst["pressure"], worst["position"]))
+    g.close()
+    o.close()

@@ -76,11 +76,42 @@ def test_noalloc_matches_allocating_solve_twice_in_a_row(lib, oracle, precision,
         assert sg["rs_final"] == sw["rs_final"]
 
 
-def test_noalloc_rejects_grids_beyond_its_limit(lib):
+@pytest.mark.parametrize("precision", [FL_CG_F32, FL_CG_F64])
+def test_noalloc_grid_changes_between_calls(lib, oracle, precision):
+    """The shared scratch keeps the last call's plan, chunk flags, exchange
+    words and vector entries: a 48^3 solve, then the 16^3 tank, then 48^3
+    again, each equal bit for bit to the allocating solve."""
     torch = pytest.importorskip("torch")
-    n = 65  # 274,625 cells > FL_NOALLOC_MAX_CELLS = 262,144
+    d48, ct48, div48, p48 = random_case()
+    d16, ct16, div16 = tank(oracle)
+    cases = [(d48, ct48, div48, p48, True, 1e-3, 120), (d16, ct16, div16, np.zeros_like(div16), False, 0.0, 40),
+             (d48, ct48, div48, p48, True, 1e-3, 120)]
+    for i, (d, ct, div, p0, warm, tol, iters) in enumerate(cases):
+        want, sw = _abi.solve_pressure(ct, div, d, 1.0, 1.0, 1.0, iters, warm_start=warm, pressure_in=p0,
+                                       tolerance=tol, precision=precision)
+        got, sg = noalloc(lib, torch, d, ct, div, p0, iters, warm, tol, precision)
+        assert np.array_equal(got, want), "call %d (%s)" % (i, d)
+        assert sg["cg_iterations"] == sw["cg_iterations"]
+
+
+def test_noalloc_rejects_overlapping_buffers(lib):
+    torch = pytest.importorskip("torch")
+    n = 16
     buf = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
     ct = torch.zeros(n ** 3, dtype=torch.uint8, device="cuda")
     r = lib.fl_solve_pressure_noalloc(n, n, n, ct.data_ptr(), buf.data_ptr(), buf.data_ptr(), 1.0, 1.0, 1.0, 10, 0,
                                       0.0, FL_CG_F32, None, None)
     assert r == FL_INVALID_ARG
+    assert b"overlap" in lib.fl_last_error(None)
+
+
+def test_noalloc_rejects_grids_beyond_its_limit(lib):
+    torch = pytest.importorskip("torch")
+    n = 65  # 274,625 cells > FL_NOALLOC_MAX_CELLS = 262,144
+    div = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
+    pres = torch.zeros(n ** 3, dtype=torch.float32, device="cuda")
+    ct = torch.zeros(n ** 3, dtype=torch.uint8, device="cuda")
+    r = lib.fl_solve_pressure_noalloc(n, n, n, ct.data_ptr(), div.data_ptr(), pres.data_ptr(), 1.0, 1.0, 1.0, 10, 0,
+                                      0.0, FL_CG_F32, None, None)
+    assert r == FL_INVALID_ARG
+    assert b"no-allocation limit" in lib.fl_last_error(None)

@@ -40,6 +40,8 @@
 // Each block lists its liquid cells with their stencil masks (k_grid_prep's
 // cinfo) in shared memory once per solve; an iteration then touches liquid
 // cells only and issues no dependent loads for topology.
+#include <cstddef>
+
 #include "fl_device.cuh"
 
 namespace fl {
@@ -50,8 +52,17 @@ constexpr uint32_t CELL_CAP = 16384;     // liquid cells listed per block
 constexpr uint32_t KCH = 2048;           // chunk ids cached per block
 constexpr uint32_t VAL_CAP = 16384;      // chunk partials staged per window
 constexpr uint32_t MAX_PASS = KCH / KT;  // cached tree passes
+// Resident operands: when a block's listed cells fit one pass of at most two
+// cells per thread and the exchange window needs at most half of `vals`, each
+// listed cell keeps {d, r, q, p} in the upper half of `vals` for the whole
+// solve (16 B per cell; the half holds 2 * CG_THREADS cells).
+constexpr uint32_t VALS_HALF = (VAL_CAP + VAL_CAP / 32) / 2;
+constexpr uint32_t RES_MAX_A = VALS_HALF - VALS_HALF / 33;  // vpos(A - 1) < VALS_HALF
 constexpr uint32_t TAG_SPAN_MAX = 1u << 30;
 constexpr int STAGE_BATCH = 8;
+// Words in flight per thread when staging the blocks' slot lines (one window:
+// at 128^3 about 2.4 words per thread, so a smaller batch frees registers).
+constexpr int LINE_BATCH = 4;
 constexpr uint32_t MAX_CG_BLOCKS = 1024;
 // Per-chunk cost in liquid-cell units for the block split (each chunk adds a
 // tree and, when sparsely filled, cells that share few cache lines).  Kept
@@ -70,13 +81,21 @@ struct CgShared {
     float seg[CHUNK];          // segment sums (cg_reduce_final.wgsl thread accumulators)
     float red[2 * CG_WARPS];   // F64: float-float warp partials; F32: one pass of chunk trees
     uint32_t wcnt[CG_WARPS];
+    float scal[4];             // scalars of an exchange, broadcast by warp 0
     uint32_t layout, nslot;              // exchange slot layout (0 plan order, 1 lines, 2 one line per block), slots used
     float thr_f;                         // f32 stopping threshold on r.r
+    float thr_dh, thr_dl;                // FL_CG_F64 stopping threshold on r.r (float-float)
+    float rs_hi, rs_lo;                  // r.r of the last exchange (rs_old); FL_CG_F32 uses rs_hi
+    // Block-uniform loop bounds, read from shared memory where used (the cell
+    // loops sit at the 64-register limit of a 1024-thread block).
+    uint32_t u_s0, u_m, u_mc, u_npc, u_ncell, u_res;
     uint32_t bstart[MAX_CG_BLOCKS + 1];  // first plan entry of every block
     uint32_t spos[MAX_CG_BLOCKS + 1];    // first exchange slot of every block
     uint16_t lineblk[VAL_CAP / 16 + MAX_CG_BLOCKS];  // line of the slot area -> owning block
 };
 static_assert(sizeof(CgShared) <= 227 * 1024, "CG shared memory exceeds the 227 KB per-block limit");
+static_assert(offsetof(CgShared, vals) % 16 == 0 && (VALS_HALF * 4) % 16 == 0, "resident operands are float4");
+static_assert(VALS_HALF + 4 * 2 * CG_THREADS <= VAL_CAP + VAL_CAP / 32, "resident operands fit the upper half");
 
 // ---------------------------------------------------------------------------
 // Tagged words
@@ -181,6 +200,9 @@ __device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool a
 // without the pad the segment sums ran 16-way bank conflicted (0.85 vs
 // 0.47 us per exchange at 128^3).
 __device__ __forceinline__ uint32_t vpos(uint32_t e) { return e + (e >> 5); }
+
+// A block-uniform value read from shared memory at its use (not kept in a register).
+__device__ __forceinline__ uint32_t vld(const uint32_t& x) { return *(const volatile uint32_t*)&x; }
 
 // cg_reduce.wgsl:38-49 over s[0..255], evaluated by one warp: lane l forms the
 // level-128 sums of indices l, l+32, l+64, l+96, the level-64 sums of l and
@@ -425,12 +447,55 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // One pass in all: non-liquid tree slots stay zero for the whole solve.
     const bool multi = npc > 1 || mc < m;
     __syncthreads();
+    // Resident operands: thread t owns listed cells t and t + CG_THREADS in
+    // both phases, so their {d, r, q, p} stay in shared memory for the whole
+    // solve.  Phase 2 then loads nothing from global memory, q is never
+    // written there, and p is written once at the end; d (phase 1) and r
+    // (phase 2) are still stored for the neighbours in other blocks.  At 128^3
+    // this took the update phase from 2300 to 1640 cycles per iteration.
+    const bool res = !multi && ncell <= 2u * CG_THREADS && A <= RES_MAX_A;
+    float4* const rv4 = reinterpret_cast<float4*>(sh.vals + VALS_HALF);
+    if (tid == 0) {
+        sh.u_s0 = s0;
+        sh.u_m = m;
+        sh.u_mc = mc;
+        sh.u_npc = npc;
+        sh.u_ncell = ncell;
+        sh.u_res = res ? 1u : 0u;
+    }
+    if (res)
+        for (uint32_t tu = tid; tu < ncell; tu += CG_THREADS) {
+            const uint32_t e = sh.cell[tu];
+            const uint32_t c = sh.chunk[e >> 18] * CHUNK + ((e >> 10) & 255u);
+            rv4[tu] = make_float4(b.dA[c], r[c], 0.0f, p[c]);
+        }
 
+    // The scalars that follow an exchange, from its sum v: post 1 alpha
+    // (cg_alpha.wgsl:17-22, sc = rs_old / v), post 2 beta and the stopping test
+    // (cg_beta.wgsl:16-30, sc = v / rs_old, dn).  Evaluated once, by lane 0 of
+    // warp 0, and broadcast through sh.scal.
+    auto post_f32 = [&](int post, float v) {
+        const float rs_old = sh.rs_hi;
+        float sc = 0.0f;
+        bool dn = false;
+        if (post == 1) sc = fabsf(v) > 1e-30f ? __fdiv_rn(rs_old, v) : 0.0f;
+        if (post != 1) sh.rs_hi = v;  // the initial r.r, or rs_new
+        if (post == 2) {
+            sc = rs_old > 1e-30f ? __fdiv_rn(v, rs_old) : 0.0f;
+            dn = stop_on && v <= sh.thr_f;
+        }
+        sh.scal[0] = v;
+        sh.scal[1] = sc;
+        sh.scal[2] = dn ? 1.0f : 0.0f;
+    };
     // FL_CG_F32 scalar: the segment sums of cg_reduce_final.wgsl over the
     // staged partials (windows of VAL_CAP entries, in plan order), then its
-    // 256-wide tree, evaluated by every warp.  `x` == nullptr: the initial
-    // residual partials part_rr, indexed by chunk.  Returns false on abort.
-    auto reduce_f32 = [&](const unsigned long long* x, uint32_t tag, bool acq, float& out) -> bool {
+    // 256-wide tree, evaluated by warp 0 (32 warps evaluating it redundantly
+    // competed for issue slots: 0.3 us per exchange at 128^3).  `x` == nullptr:
+    // the initial residual partials part_rr, indexed by chunk.  Every thread
+    // receives the sum (out) and the post scalars (sc, dn).  Returns false on abort.
+    auto reduce_f32 = [&](const unsigned long long* x, uint32_t tag, bool acq, int post, float& out, float& sc,
+                          bool& dn) -> bool {
         float acc = 0.0f;
         bool ok = true;
         const uint32_t A = sh.off[CHUNK];
@@ -440,11 +505,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                                          // out rather than through stage_words: measured 0.5 ms/step faster.
                 const uint32_t nslot_used = sh.nslot;
                 const bool one_line = sh.layout == 2u;
-                for (uint32_t v0 = tid; v0 < nslot_used; v0 += STAGE_BATCH * CG_THREADS) {
-                    unsigned long long w[STAGE_BATCH];
-                    uint32_t dst[STAGE_BATCH];
+                for (uint32_t v0 = tid; v0 < nslot_used; v0 += LINE_BATCH * CG_THREADS) {
+                    unsigned long long w[LINE_BATCH];
+                    uint32_t dst[LINE_BATCH];
 #pragma unroll
-                    for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
+                    for (int k2 = 0; k2 < LINE_BATCH; k2++) {
                         const uint32_t v = v0 + k2 * CG_THREADS;
                         const uint32_t bb = v < nslot_used ? (one_line ? v >> 4 : (uint32_t)sh.lineblk[v >> 4]) : 0u;
                         const uint32_t j = v - sh.spos[bb];
@@ -453,7 +518,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         w[k2] = use ? ld_tag(x + v, acq) : 0ull;
                     }
 #pragma unroll
-                    for (int k2 = 0; k2 < STAGE_BATCH; k2++) {
+                    for (int k2 = 0; k2 < LINE_BATCH; k2++) {
                         if (dst[k2] != 0xffffffffu && ok) {
                             if ((uint32_t)(w[k2] >> 32) != tag) {
                                 w[k2] = wait_tag(x + v0 + k2 * CG_THREADS, tag, st, acq, b.prm);
@@ -488,21 +553,52 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         }
         if (tid < (uint32_t)CHUNK) sh.seg[tid] = acc;
         __syncthreads();
-        out = __shfl_sync(0xffffffffu, chunk_tree(sh.seg, lane), 0);
+        if (warp == 0) {
+            const float v = chunk_tree(sh.seg, lane);
+            if (lane == 0) post_f32(post, v);
+        }
+        __syncthreads();
+        out = sh.scal[0];
+        sc = sh.scal[1];
+        dn = sh.scal[2] != 0.0f;
         return true;
     };
     // FL_CG_F64 scalar: the blocks' float-float partials (two words of block b
-    // at 16*b), summed by every warp in the same fixed order (lanes stride
-    // over blocks, then a shuffle tree), so no broadcast is needed.
-    auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, Df& out) -> bool {
+    // at 16*b), summed by warp 0 in a fixed order (lanes stride over blocks,
+    // then a shuffle tree); lane 0 evaluates the post scalars (alpha, or beta
+    // and the stopping test, from rs_old) and broadcasts them with the sum.
+    auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, int post, Df& out, float& sc,
+                         bool& dn) -> bool {
         const bool ok = stage_words(
             2 * G, tag, acq, st, b.prm, sh.vals,
             [&](uint32_t v) -> const unsigned long long* { return words + (v >> 1) * 16u + (v & 1u); },
             [&](uint32_t v) -> uint32_t { return v; });
         if (__syncthreads_or(!ok)) return false;
-        Df acc = {0.0f, 0.0f};
-        for (uint32_t bb = lane; bb < G; bb += 32) acc = df_add(acc, Df{sh.vals[2 * bb], sh.vals[2 * bb + 1]});
-        out = warp_allsum_df(acc);
+        if (warp == 0) {
+            Df acc = {0.0f, 0.0f};
+            for (uint32_t bb = lane; bb < G; bb += 32) acc = df_add(acc, Df{sh.vals[2 * bb], sh.vals[2 * bb + 1]});
+            acc = warp_sum_df(acc);
+            if (lane == 0) {
+                const Df rs_old = {sh.rs_hi, sh.rs_lo};
+                float scv = 0.0f;
+                bool d2 = false;
+                if (post == 1) scv = fabsf(acc.hi) > 1e-30f ? df_div(rs_old, acc) : 0.0f;
+                if (post == 2) {
+                    scv = rs_old.hi > 1e-30f ? df_div(acc, rs_old) : 0.0f;
+                    d2 = stop_on && df_le(acc, Df{sh.thr_dh, sh.thr_dl});
+                    sh.rs_hi = acc.hi;
+                    sh.rs_lo = acc.lo;
+                }
+                sh.scal[0] = acc.hi;
+                sh.scal[1] = acc.lo;
+                sh.scal[2] = scv;
+                sh.scal[3] = d2 ? 1.0f : 0.0f;
+            }
+        }
+        __syncthreads();
+        out = Df{sh.scal[0], sh.scal[1]};
+        sc = sh.scal[2];
+        dn = sh.scal[3] != 0.0f;
         return true;
     };
     // Block float-float partial published as two tagged words on the block's line.
@@ -553,8 +649,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     };
 
     // Initial residual norm (cg_init.wgsl + cg_reduce of r.r).
-    float rs_old_f = 0.0f, rs_init_f = 0.0f;
-    Df rs_old_d = {0.0f, 0.0f}, rs_init_d = {0.0f, 0.0f}, thr_d = {0.0f, 0.0f};
+    float rs_init_f = 0.0f;
+    Df rs_init_d = {0.0f, 0.0f};
     if (f64) {
         Df acc = {0.0f, 0.0f};
         for (uint32_t e = tid; e < A; e += CG_THREADS) {
@@ -567,15 +663,20 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             sh.red[2 * warp + 1] = acc.lo;
         }
         __syncthreads();
-        rs_old_d = rs_init_d = warp_allsum_df(Df{sh.red[2 * lane], sh.red[2 * lane + 1]});
+        rs_init_d = warp_allsum_df(Df{sh.red[2 * lane], sh.red[2 * lane + 1]});
         // stopping threshold tol^2 * rs_init (or the absolute one), once per solve
-        const double thr = P.thr_abs ? P.thr_abs_d : tol_sq_d * df_to_double(rs_init_d);
-        thr_d.hi = (float)thr;
-        thr_d.lo = (float)(thr - (double)thr_d.hi);
+        if (tid == 0) {
+            sh.rs_hi = rs_init_d.hi;
+            sh.rs_lo = rs_init_d.lo;
+            const double thr = P.thr_abs ? P.thr_abs_d : tol_sq_d * df_to_double(rs_init_d);
+            sh.thr_dh = (float)thr;
+            sh.thr_dl = (float)(thr - (double)sh.thr_dh);
+        }
         __syncthreads();  // sh.red is reused
     } else {
-        reduce_f32(nullptr, 0u, false, rs_old_f);
-        rs_init_f = rs_old_f;
+        float sc0;
+        bool dn0;
+        reduce_f32(nullptr, 0u, false, 0, rs_init_f, sc0, dn0);  // also sets sh.rs_hi
     }
     // Thresholds and rs_init are stored once here, not held in registers
     // through the loop.  f32: tol^2 * rs_init (cg_beta.wgsl:25-30) or the
@@ -596,10 +697,53 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         // ---------------- phase 1: direction + SpMV + d.q ----------------
         Df acc = {0.0f, 0.0f};
         tag++;
-        {
+        if (vld(sh.u_res)) {  // resident operands: own d, r from shared memory, neighbours' from global
+            uint32_t ent[2], cc[2];
+            float rv[2][7], dv[2][7];
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const uint32_t tu = tid + u * CG_THREADS;
+                const bool ok = tu < vld(sh.u_ncell);
+                ent[u] = ok ? sh.cell[tu] : 0u;
+                cc[u] = sh.chunk[ent[u] >> 18] * CHUNK + ((ent[u] >> 10) & 255u);
+                const uint32_t c = cc[u];
+                const float2 own = ok ? *reinterpret_cast<const float2*>(&rv4[tu]) : make_float2(0.0f, 0.0f);
+                dv[u][0] = own.x;
+                rv[u][0] = own.y;
+                const uint32_t nb6[6] = {c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
+#pragma unroll
+                for (int s = 1; s < 7; s++) {
+                    const bool need = ok && ((ent[u] >> s) & 1u);
+                    dv[u][s] = need ? d_src[nb6[s - 1]] : 0.0f;
+                    rv[u][s] = (need && !first) ? r[nb6[s - 1]] : 0.0f;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const uint32_t tu = tid + u * CG_THREADS;
+                if (tu >= vld(sh.u_ncell)) continue;
+                const uint32_t info = ent[u];
+                const float dc = first ? dv[u][0] : __fadd_rn(rv[u][0], __fmul_rn(beta, dv[u][0]));  // cg_dir.wgsl:30
+                float sum = 0.0f;
+#pragma unroll
+                for (int s = 1; s < 7; s++) {
+                    if ((info >> s) & 1u) {
+                        const float dn = first ? dv[u][s] : __fadd_rn(rv[u][s], __fmul_rn(beta, dv[u][s]));
+                        sum = __fadd_rn(sum, dn);
+                    }
+                }
+                const float qc = __fsub_rn(__fmul_rn((float)((info >> 7) & 7u), dc), sum);  // cg_spmv.wgsl:46-68
+                if (!first) d_cur[cc[u]] = dc;
+                rv4[tu].x = dc;
+                rv4[tu].z = qc;
+                if (f64) acc = df_add(acc, df_prod(dc, qc));
+                else sh.tree[info >> 18][(info >> 10) & 255u] = __fmul_rn(dc, qc);
+            }
+            if (!f64) publish_trees(0, vld(sh.u_mc), slotA, tag, false);
+        } else {
             uint32_t j0 = 0;
-            for (uint32_t ps = 0; ps < npc; ps++, j0 += KT) {
-                const uint32_t nb = mc - j0 < KT ? mc - j0 : KT;
+            for (uint32_t ps = 0; ps < vld(sh.u_npc); ps++, j0 += KT) {
+                const uint32_t nb = vld(sh.u_mc) - j0 < KT ? vld(sh.u_mc) - j0 : KT;
                 if (multi && !f64) {
                     for (uint32_t i = tid; i < nb * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
                     __syncthreads();
@@ -650,14 +794,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 }
                 if (!f64) {
                     publish_trees(j0, nb, slotA, tag, false);
-                    if (ps + 1 < npc || mc < m) __syncthreads();
+                    if (ps + 1 < vld(sh.u_npc) || vld(sh.u_mc) < vld(sh.u_m)) __syncthreads();
                 }
             }
-            for (j0 = mc; j0 < m; j0 += KT) {  // chunks beyond the list: one cell slot per thread
-                const uint32_t nb = m - j0 < KT ? m - j0 : KT;
+            for (j0 = vld(sh.u_mc); j0 < vld(sh.u_m); j0 += KT) {  // chunks beyond the list: one cell slot per thread
+                const uint32_t nb = vld(sh.u_m) - j0 < KT ? vld(sh.u_m) - j0 : KT;
                 for (uint32_t t = tid; t < nb * CHUNK; t += CG_THREADS) {
                     const uint32_t j = j0 + t / CHUNK, cl = t & (CHUNK - 1);
-                    const uint32_t chunk = j < KCH ? sh.chunk[j] : plan[s0 + j];
+                    const uint32_t chunk = j < KCH ? sh.chunk[j] : plan[vld(sh.u_s0) + j];
                     const uint32_t c = chunk * CHUNK + cl;
                     const uint32_t info = c < C ? cinfo[c] : 0u;
                     float prod = 0.0f;
@@ -688,23 +832,40 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             }
         }
         float alpha;
-        if (f64) {
-            publish_df(acc, wordA, tag, false);
-            Df dq;
-            if (!reduce_df(wordA, tag, false, dq)) return;
-            alpha = fabsf(dq.hi) > 1e-30f ? df_div(rs_old_d, dq) : 0.0f;
-        } else {
-            float dq;
-            if (!reduce_f32(slotA, tag, false, dq)) return;
-            alpha = fabsf(dq) > 1e-30f ? __fdiv_rn(rs_old_f, dq) : 0.0f;  // cg_alpha.wgsl:17-22
+        {
+            bool dn_unused;
+            if (f64) {
+                publish_df(acc, wordA, tag, false);
+                Df dq;
+                if (!reduce_df(wordA, tag, false, 1, dq, alpha, dn_unused)) return;
+            } else {
+                float dq;
+                if (!reduce_f32(slotA, tag, false, 1, dq, alpha, dn_unused)) return;
+            }
         }
         // ---------------- phase 2: update + r.r ----------------
         acc = {0.0f, 0.0f};
         tag++;
-        {
+        if (vld(sh.u_res)) {  // every operand in shared memory; r also to global for the neighbours
+#pragma unroll
+            for (int u = 0; u < 2; u++) {
+                const uint32_t tu = tid + u * CG_THREADS;
+                if (tu >= vld(sh.u_ncell)) continue;
+                const uint32_t e = sh.cell[tu];
+                const float4 o = rv4[tu];
+                const float pn = __fadd_rn(o.w, __fmul_rn(alpha, o.x));  // cg_update.wgsl:33
+                const float rc = __fsub_rn(o.y, __fmul_rn(alpha, o.z));  // cg_update.wgsl:34
+                r[sh.chunk[e >> 18] * CHUNK + ((e >> 10) & 255u)] = rc;
+                rv4[tu].y = rc;
+                rv4[tu].w = pn;
+                if (f64) acc = df_add(acc, df_prod(rc, rc));
+                else sh.tree[e >> 18][(e >> 10) & 255u] = __fmul_rn(rc, rc);
+            }
+            if (!f64) publish_trees(0, vld(sh.u_mc), slotB, tag, true);
+        } else {
             uint32_t j0 = 0;
-            for (uint32_t ps = 0; ps < npc; ps++, j0 += KT) {
-                const uint32_t nb = mc - j0 < KT ? mc - j0 : KT;
+            for (uint32_t ps = 0; ps < vld(sh.u_npc); ps++, j0 += KT) {
+                const uint32_t nb = vld(sh.u_mc) - j0 < KT ? vld(sh.u_mc) - j0 : KT;
                 if (multi && !f64) {
                     for (uint32_t i = tid; i < nb * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
                     __syncthreads();
@@ -737,14 +898,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 }
                 if (!f64) {
                     publish_trees(j0, nb, slotB, tag, true);
-                    if (ps + 1 < npc || mc < m) __syncthreads();
+                    if (ps + 1 < vld(sh.u_npc) || vld(sh.u_mc) < vld(sh.u_m)) __syncthreads();
                 }
             }
-            for (j0 = mc; j0 < m; j0 += KT) {
-                const uint32_t nb = m - j0 < KT ? m - j0 : KT;
+            for (j0 = vld(sh.u_mc); j0 < vld(sh.u_m); j0 += KT) {
+                const uint32_t nb = vld(sh.u_m) - j0 < KT ? vld(sh.u_m) - j0 : KT;
                 for (uint32_t t = tid; t < nb * CHUNK; t += CG_THREADS) {
                     const uint32_t j = j0 + t / CHUNK, cl = t & (CHUNK - 1);
-                    const uint32_t chunk = j < KCH ? sh.chunk[j] : plan[s0 + j];
+                    const uint32_t chunk = j < KCH ? sh.chunk[j] : plan[vld(sh.u_s0) + j];
                     const uint32_t c = chunk * CHUNK + cl;
                     const uint32_t info = c < C ? cinfo[c] : 0u;
                     float prod = 0.0f;
@@ -768,22 +929,21 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         if (f64) {
             publish_df(acc, wordB, tag, true);
             Df rs_new;
-            if (!reduce_df(wordB, tag, true, rs_new)) return;
-            beta = rs_old_d.hi > 1e-30f ? df_div(rs_new, rs_old_d) : 0.0f;
-            rs_old_d = rs_new;
-            done = stop_on && df_le(rs_new, thr_d);
+            if (!reduce_df(wordB, tag, true, 2, rs_new, beta, done)) return;
         } else {
             float rs_new;
-            if (!reduce_f32(slotB, tag, true, rs_new)) return;
-            beta = rs_old_f > 1e-30f ? __fdiv_rn(rs_new, rs_old_f) : 0.0f;  // cg_beta.wgsl:16-23
-            rs_old_f = rs_new;
-            done = stop_on && rs_new <= sh.thr_f;
+            if (!reduce_f32(slotB, tag, true, 2, rs_new, beta, done)) return;
         }
         if (done) break;
     }
+    if (res)  // the resident pressure, once
+        for (uint32_t tu = tid; tu < ncell; tu += CG_THREADS) {
+            const uint32_t e = sh.cell[tu];
+            p[sh.chunk[e >> 18] * CHUNK + ((e >> 10) & 255u)] = rv4[tu].w;
+        }
     if (blockIdx.x == 0 && tid == 0) {
         st->cg_iters = k;
-        st->rs_final = f64 ? df_to_double(rs_old_d) : (double)rs_old_f;
+        st->rs_final = f64 ? df_to_double(Df{sh.rs_hi, sh.rs_lo}) : (double)sh.rs_hi;
     }
 }
 

@@ -406,6 +406,8 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     unsigned long long* slotB = slotA + nslot;     // r.r chunk partials
     unsigned long long* wordA = slotB + nslot;     // FL_CG_F64: {hi, lo} of block b at 16*b
     unsigned long long* wordB = wordA + 16 * (size_t)G;
+    unsigned long long* segA = wordB + 16 * (size_t)G;  // two-hop exchanges: 256 segment sums each
+    unsigned long long* segB = segA + CHUNK;
     const uint32_t mch = m < KCH ? m : KCH;
     for (uint32_t j = tid; j < mch; j += CG_THREADS) sh.chunk[j] = plan[s0 + j];
     for (uint32_t i = tid; i < KT * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
@@ -488,17 +490,75 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         sh.scal[1] = sc;
         sh.scal[2] = dn ? 1.0f : 0.0f;
     };
-    // FL_CG_F32 scalar: the segment sums of cg_reduce_final.wgsl over the
-    // staged partials (windows of VAL_CAP entries, in plan order), then its
+    // FL_CG_F32 scalar: the segment sums of cg_reduce_final.wgsl, then its
     // 256-wide tree, evaluated by warp 0 (32 warps evaluating it redundantly
-    // competed for issue slots: 0.3 us per exchange at 128^3).  `x` == nullptr:
-    // the initial residual partials part_rr, indexed by chunk.  Every thread
-    // receives the sum (out) and the post scalars (sc, dn).  Returns false on abort.
-    auto reduce_f32 = [&](const unsigned long long* x, uint32_t tag, bool acq, int post, float& out, float& sc,
-                          bool& dn) -> bool {
+    // competed for issue slots: 0.3 us per exchange at 128^3).  Every thread
+    // receives the sum (out) and the post scalars (sc, dn).  Returns false on
+    // abort.  Three ways to the segment sums:
+    //  * line layouts (all partials fit one window): every block stages every
+    //    block's slot line and sums all 256 segments itself (one hop);
+    //  * plan-order layout (more active chunks than one window: every block
+    //    reading every partial cost 6-9 us per exchange at 256^3): two hops.
+    //    Block bb owns segments bb, bb + G, ...; one warp per owned segment
+    //    polls its partials (plan entries off[li]..off[li+1]), sums them in
+    //    order in lane 0 and publishes the segment sum as a tagged word in
+    //    `segw` (release on the exchange after which vector writes are read:
+    //    the owners' acquires and releases carry every block's writes on);
+    //    then every block polls the 256 segment words;
+    //  * `x` == nullptr: the initial residual partials part_rr, indexed by
+    //    chunk, staged in windows.
+    auto reduce_f32 = [&](const unsigned long long* x, unsigned long long* segw, uint32_t tag, bool acq, int post,
+                          float& out, float& sc, bool& dn) -> bool {
         float acc = 0.0f;
         bool ok = true;
         const uint32_t A = sh.off[CHUNK];
+        if (x && sh.layout == 0u) {
+            float* buf = sh.vals + warp * 128u;  // per-warp staging of 128 partials
+            for (uint32_t li = blockIdx.x + warp * G; li < (uint32_t)CHUNK; li += CG_WARPS * G) {
+                const uint32_t lo = sh.off[li], hi = sh.off[li + 1];
+                float s = 0.0f;
+                for (uint32_t e0 = lo; e0 < hi; e0 += 128u) {
+#pragma unroll
+                    for (int k2 = 0; k2 < 4; k2++) {
+                        const uint32_t e = e0 + lane + 32u * k2;
+                        unsigned long long w = 0ull;
+                        if (e < hi) {
+                            w = ld_tag(x + e, acq);
+                            if ((uint32_t)(w >> 32) != tag && ok) {
+                                w = wait_tag(x + e, tag, st, acq, b.prm);
+                                ok = (uint32_t)(w >> 32) == tag;
+                            }
+                        }
+                        buf[lane + 32u * k2] = __uint_as_float((uint32_t)w);
+                    }
+                    __syncwarp();
+                    if (lane == 0) {  // cg_reduce_final.wgsl:29-36: in plan order, from +0
+                        const uint32_t n = hi - e0 < 128u ? hi - e0 : 128u;
+                        uint32_t j = 0;
+                        for (; j + 8 <= n; j += 8) {
+                            float t8[8];
+#pragma unroll
+                            for (int k2 = 0; k2 < 8; k2++) t8[k2] = buf[j + k2];
+#pragma unroll
+                            for (int k2 = 0; k2 < 8; k2++) s = __fadd_rn(s, t8[k2]);
+                        }
+                        for (; j < n; j++) s = __fadd_rn(s, buf[j]);
+                    }
+                    __syncwarp();
+                }
+                // a segment whose partials did not all arrive is not published
+                if (__all_sync(0xffffffffu, ok) && lane == 0) publish(segw + li, tag, s, acq);
+            }
+            if (tid < (uint32_t)CHUNK) {
+                unsigned long long w = ld_tag(segw + tid, acq);
+                if ((uint32_t)(w >> 32) != tag && ok) {
+                    w = wait_tag(segw + tid, tag, st, acq, b.prm);
+                    ok = (uint32_t)(w >> 32) == tag;
+                }
+                sh.seg[tid] = __uint_as_float((uint32_t)w);
+            }
+            if (__syncthreads_or(!ok)) return false;
+        } else {
         for (uint32_t w0 = 0; w0 < A; w0 += VAL_CAP) {
             const uint32_t wn = A - w0 < VAL_CAP ? A - w0 : VAL_CAP;
             if (x && sh.layout != 0u) {  // one window (A <= VAL_CAP): walk the blocks' lines.  Written
@@ -528,10 +588,6 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         }
                     }
                 }
-            } else if (x) {  // plan order, window [w0, w0 + wn)
-                ok = stage_words(
-                    wn, tag, acq, st, b.prm, sh.vals, [&](uint32_t v) -> const unsigned long long* { return x + w0 + v; },
-                    [&](uint32_t v) -> uint32_t { return vpos(v); });
             } else {
                 for (uint32_t i = tid; i < wn; i += CG_THREADS) sh.vals[vpos(i)] = b.part_rr[plan[w0 + i]];
             }
@@ -553,6 +609,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         }
         if (tid < (uint32_t)CHUNK) sh.seg[tid] = acc;
         __syncthreads();
+        }
         if (warp == 0) {
             const float v = chunk_tree(sh.seg, lane);
             if (lane == 0) post_f32(post, v);
@@ -676,7 +733,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     } else {
         float sc0;
         bool dn0;
-        reduce_f32(nullptr, 0u, false, 0, rs_init_f, sc0, dn0);  // also sets sh.rs_hi
+        reduce_f32(nullptr, nullptr, 0u, false, 0, rs_init_f, sc0, dn0);  // also sets sh.rs_hi
     }
     // Thresholds and rs_init are stored once here, not held in registers
     // through the loop.  f32: tol^2 * rs_init (cg_beta.wgsl:25-30) or the
@@ -840,7 +897,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 if (!reduce_df(wordA, tag, false, 1, dq, alpha, dn_unused)) return;
             } else {
                 float dq;
-                if (!reduce_f32(slotA, tag, false, 1, dq, alpha, dn_unused)) return;
+                if (!reduce_f32(slotA, segA, tag, false, 1, dq, alpha, dn_unused)) return;
             }
         }
         // ---------------- phase 2: update + r.r ----------------
@@ -932,7 +989,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             if (!reduce_df(wordB, tag, true, 2, rs_new, beta, done)) return;
         } else {
             float rs_new;
-            if (!reduce_f32(slotB, tag, true, 2, rs_new, beta, done)) return;
+            if (!reduce_f32(slotB, segB, tag, true, 2, rs_new, beta, done)) return;
         }
         if (done) break;
     }

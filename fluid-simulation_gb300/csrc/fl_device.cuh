@@ -115,7 +115,7 @@ struct DevBufs {
 #endif
 FL_HD constexpr size_t cg_plan_words(size_t max_blocks) { return (size_t)CHUNK + 3 + 2 * (max_blocks + 1); }
 FL_HD constexpr size_t cg_x_words(size_t nchunks, size_t max_blocks) {
-    return 16 + 2 * ((nchunks + 15) & ~(size_t)15) + 64 * max_blocks;
+    return 16 + 2 * ((nchunks + 15) & ~(size_t)15) + 64 * max_blocks + 2 * 256;
 }
 
 // Buffers of one adjoint step (fl_adjoint.cu).

@@ -11,10 +11,11 @@
 // solve as the exact linear solve A p = b (A symmetric), so its adjoint is a
 // second CG solve with the same operator.  Stages, in reverse order:
 //
-//   k_adj_g2p       g2p.wgsl:131-198 (forward Euler, friction off): particle
-//                   gradients w.r.t. position and velocity, and face gradients
-//                   of the final and saved velocities (scatter = transpose of
-//                   the trilinear gather; one float2 vector atomic per tap into
+//   k_adj_g2p       g2p.wgsl:131-198 (friction band, speed clamp, forward Euler
+//                   or the midpoint step, wall clamp): particle gradients
+//                   w.r.t. position and velocity, and face gradients of the
+//                   final and saved velocities (scatter = transpose of the
+//                   trilinear gather; one float2 vector atomic per tap into
 //                   the interleaved {final, saved} gradients)
 //   k_adj_prhs      gradient.wgsl transposed: dL/dp per liquid cell, the RHS
 //                   of the adjoint pressure solve A lambda = dL/dp
@@ -104,94 +105,224 @@ __device__ __forceinline__ void stencil(const DevParams& P, int axis, const floa
 }
 
 // ---------------------------------------------------------------------------
-// G2P + advection adjoint (forward Euler, no friction).
+// G2P + advection adjoint.
 
+// Wall-aware renormalised gather of the final (and saved) face velocities at
+// cell-space point q (g2p.wgsl:56-129), with the position derivatives of the
+// quotients per unit world coordinate.  W = sum of weights (0: no tap).
+template <bool WITH_SAVED>
+__device__ __forceinline__ void gather_d(const AdjBufs& a, const DevParams& P, const float q[3], float val[3],
+                                         float dval[3][3], float sav[3], float dsav[3][3], float W[3]) {
+    #pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        float fsum = 0.0f, ssum = 0.0f, wsum = 0.0f, dws[3] = {0, 0, 0}, dfs[3] = {0, 0, 0}, dss[3] = {0, 0, 0};
+        const float* fv = a.fin[ax];
+        const float* svv = a.sav[ax];
+        stencil(P, ax, q, true, [&](size_t idx, float w, const float* dw) {
+            const float f = fv[idx];
+            fsum += w * f;
+            wsum += w;
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {
+                dws[b] += dw[b];
+                dfs[b] += dw[b] * f;
+            }
+            if (WITH_SAVED) {
+                const float s = svv[idx];
+                ssum += w * s;
+                #pragma unroll
+                for (int b = 0; b < 3; b++) dss[b] += dw[b] * s;
+            }
+        });
+        W[ax] = wsum;
+        if (wsum > 0.0f) {
+            val[ax] = fsum / wsum;
+            if (WITH_SAVED) sav[ax] = ssum / wsum;
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {  // d(F/W) = (dF - (F/W) dW)/W, per unit cell coordinate
+                dval[ax][b] = (dfs[b] - val[ax] * dws[b]) / wsum * P.inv_h;
+                if (WITH_SAVED) dsav[ax][b] = (dss[b] - sav[ax] * dws[b]) / wsum * P.inv_h;
+            }
+        } else {
+            val[ax] = 0.0f;
+            if (WITH_SAVED) sav[ax] = 0.0f;
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {
+                dval[ax][b] = 0.0f;
+                if (WITH_SAVED) dsav[ax][b] = 0.0f;
+            }
+        }
+    }
+}
+
+// The speed clamp v * maxs/|v| (g2p.wgsl:159-162): forward factor and the
+// gradient of its input from the gradient g of its output.
+struct Clamp {
+    float sp, sc;
+    bool on;
+};
+__device__ __forceinline__ Clamp clamp_fwd(const float v[3], float maxs) {
+    Clamp c;
+    c.sp = sqrtf(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    c.on = c.sp > maxs && c.sp > 0.0f;
+    c.sc = c.on ? maxs / c.sp : 1.0f;
+    return c;
+}
+__device__ __forceinline__ void clamp_bwd(const Clamp& c, const float v[3], const float g[3], float out[3]) {
+    if (c.on) {
+        const float inv = 1.0f / c.sp;
+        const float dotp = (g[0] * v[0] + g[1] * v[1] + g[2] * v[2]) * inv * inv;
+        #pragma unroll
+        for (int b = 0; b < 3; b++) out[b] = c.sc * (g[b] - v[b] * dotp);
+    } else {
+        #pragma unroll
+        for (int b = 0; b < 3; b++) out[b] = g[b];
+    }
+}
+
+// Face gradients of a wall-aware gather at q: d(sum w f / W)/d f = w/W.
+__device__ __forceinline__ void scatter_faces(const AdjBufs& a, const DevParams& P, const float q[3], const float W[3],
+                                              const float gfin[3], const float gsav[3]) {
+    #pragma unroll
+    for (int ax = 0; ax < 3; ax++) {
+        if (!(W[ax] > 0.0f)) continue;
+        const float cf = gfin[ax] / W[ax], cs = gsav ? gsav[ax] / W[ax] : 0.0f;
+        if (cf == 0.0f && cs == 0.0f) continue;
+        float2* gfs = a.g_fs[ax];
+        stencil(P, ax, q, true, [&](size_t idx, float w, const float*) {
+            atomicAdd(gfs + idx, make_float2(w * cf, w * cs));
+        });
+    }
+}
+
+// g2p.wgsl:131-198 and the midpoint option, in reverse.  Forward recomputed
+// per particle: PIC and saved gathers at X, mix, speed clamp, the friction
+// band factors (g2p.wgsl:173-184), then forward Euler (g2p.wgsl:186) or the
+// midpoint step (k1 = clamp(PIC(X)), Xm = X + k1 dt/2, k2 = clamp(fin(Xm)),
+// X' = X + k2 dt) and the wall clamp (g2p.wgsl:189-194).  The discrete choices
+// of the recorded step are held fixed: which clamps are active, which side of
+// the band's min and which axis of the band's max are taken, which components
+// are pinned to the walls.
 __global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
     const DevParams& P = *a.prm;
     const uint32_t n = P.n;
-    const float alpha = P.flip, dt = P.dt, maxs = P.maxs, inv_h = P.inv_h;
+    const float alpha = P.flip, dt = P.dt, maxs = P.maxs, inv_h = P.inv_h, friction = P.friction;
+    const bool rk2 = P.advect_order == 2u;
     for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
         const float4 pos = a.part[2 * (size_t)d], pvel = a.part[2 * (size_t)d + 1];
         const float X[3] = {pos.x, pos.y, pos.z}, pv[3] = {pvel.x, pvel.y, pvel.z};
         const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
-        // forward recompute: pic, saved, their position derivatives
         float pic[3], sv[3], dpic[3][3], dsv[3][3], W[3];
-        for (int ax = 0; ax < 3; ax++) {
-            float fsum = 0.0f, ssum = 0.0f, wsum = 0.0f, dws[3] = {0, 0, 0}, dfs[3] = {0, 0, 0}, dss[3] = {0, 0, 0};
-            const float* fv = a.fin[ax];
-            const float* svv = a.sav[ax];
-            stencil(P, ax, q, true, [&](size_t idx, float w, const float* dw) {
-                const float f = fv[idx], s = svv[idx];
-                fsum += w * f;
-                ssum += w * s;
-                wsum += w;
-                for (int b = 0; b < 3; b++) {
-                    dws[b] += dw[b];
-                    dfs[b] += dw[b] * f;
-                    dss[b] += dw[b] * s;
-                }
-            });
-            W[ax] = wsum;
-            if (wsum > 0.0f) {
-                pic[ax] = fsum / wsum;
-                sv[ax] = ssum / wsum;
-                for (int b = 0; b < 3; b++) {  // d(F/W) = (dF - (F/W) dW)/W, per unit cell coordinate
-                    dpic[ax][b] = (dfs[b] - pic[ax] * dws[b]) / wsum * inv_h;
-                    dsv[ax][b] = (dss[b] - sv[ax] * dws[b]) / wsum * inv_h;
-                }
-            } else {
-                pic[ax] = sv[ax] = 0.0f;
-                for (int b = 0; b < 3; b++) dpic[ax][b] = dsv[ax][b] = 0.0f;
+        gather_d<true>(a, P, q, pic, dpic, sv, dsv, W);
+        float mix[3];
+        #pragma unroll
+        for (int b = 0; b < 3; b++) mix[b] = pic[b] * (1.0f - alpha) + (pv[b] + (pic[b] - sv[b])) * alpha;
+        const Clamp cm = clamp_fwd(mix, maxs);
+        float nvc[3];  // after the speed clamp, before friction
+        #pragma unroll
+        for (int b = 0; b < 3; b++) nvc[b] = mix[b] * cm.sc;
+        // friction: nv_b = nvc_b (1 - friction max(nr_c, nr_d)), nr_a = clamp(1 - min(dlo, dhi), 0, 1)
+        float ff[3] = {1.0f, 1.0f, 1.0f}, dnr[3] = {0.0f, 0.0f, 0.0f};
+        int fsel[3] = {-1, -1, -1};
+        if (friction > 0.0f) {
+            const float band = P.h * 2.5f;
+            float nr[3];
+            #pragma unroll
+            for (int c = 0; c < 3; c++) {
+                const float dlo = (X[c] - P.lo[c]) / band, dhi = (P.hi[c] - X[c]) / band;
+                const float u = 1.0f - fminf(dlo, dhi);
+                nr[c] = fminf(fmaxf(u, 0.0f), 1.0f);
+                dnr[c] = (u > 0.0f && u < 1.0f) ? (dlo <= dhi ? -1.0f / band : 1.0f / band) : 0.0f;
+            }
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {
+                const int c1 = b == 0 ? 1 : 0, c2 = b == 2 ? 1 : 2;
+                const bool first_max = nr[c1] >= nr[c2];
+                fsel[b] = first_max ? c1 : c2;
+                ff[b] = 1.0f - friction * (first_max ? nr[c1] : nr[c2]);
             }
         }
-        float mix[3];
-        for (int b = 0; b < 3; b++) mix[b] = pic[b] * (1.0f - alpha) + (pv[b] + (pic[b] - sv[b])) * alpha;
-        const float sp = sqrtf(mix[0] * mix[0] + mix[1] * mix[1] + mix[2] * mix[2]);
-        const bool clamped = sp > maxs && sp > 0.0f;
-        const float sc = clamped ? maxs / sp : 1.0f;
         float nv[3], np[3];
-        bool wall[3];
-        for (int b = 0; b < 3; b++) {
-            nv[b] = mix[b] * sc;
-            np[b] = X[b] + nv[b] * dt;
-            wall[b] = np[b] < P.lo[b] || np[b] > P.hi[b];
+        #pragma unroll
+        for (int b = 0; b < 3; b++) nv[b] = nvc[b] * ff[b];
+        // advection
+        float qm[3], pic2[3], dpic2[3][3], W2[3], k1[3], k2[3];
+        Clamp c1 = {0.0f, 1.0f, false}, c2 = {0.0f, 1.0f, false};
+        if (rk2) {
+            c1 = clamp_fwd(pic, maxs);
+            float Xm[3];
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {
+                k1[b] = pic[b] * c1.sc;
+                Xm[b] = X[b] + k1[b] * P.half_dt;
+                qm[b] = (Xm[b] - P.origin[b]) * inv_h;
+            }
+            gather_d<false>(a, P, qm, pic2, dpic2, nullptr, nullptr, W2);
+            c2 = clamp_fwd(pic2, maxs);
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {
+                k2[b] = pic2[b] * c2.sc;
+                np[b] = X[b] + k2[b] * dt;
+            }
+        } else {
+            #pragma unroll
+            for (int b = 0; b < 3; b++) np[b] = X[b] + nv[b] * dt;
         }
-        // backward
+        bool wall[3];
+        #pragma unroll
+        for (int b = 0; b < 3; b++) wall[b] = np[b] < P.lo[b] || np[b] > P.hi[b];
+        // ---- backward
         const float4 g0 = a.g_out[2 * (size_t)d], g1 = a.g_out[2 * (size_t)d + 1];
-        const float gnp[3] = {g0.x, g0.y, g0.z}, gnv_out[3] = {g1.x, g1.y, g1.z};
-        float gX[3], gnv[3];
+        const float gnp_o[3] = {g0.x, g0.y, g0.z}, gnv_o[3] = {g1.x, g1.y, g1.z};
+        float gX[3], gnp[3], gnv[3], gpic_k1[3] = {0.0f, 0.0f, 0.0f};
+        #pragma unroll
+        for (int b = 0; b < 3; b++) {  // a pinned component: position at the wall, velocity zero
+            gnp[b] = wall[b] ? 0.0f : gnp_o[b];
+            gX[b] = gnp[b];
+            gnv[b] = (wall[b] ? 0.0f : gnv_o[b]) + (rk2 ? 0.0f : gnp[b] * dt);
+        }
+        if (rk2) {
+            float gk2[3], gpic2[3], gk1[3];
+            #pragma unroll
+            for (int b = 0; b < 3; b++) gk2[b] = gnp[b] * dt;
+            clamp_bwd(c2, pic2, gk2, gpic2);
+            float gXm[3] = {0.0f, 0.0f, 0.0f};
+            #pragma unroll
+            for (int b = 0; b < 3; b++)
+                #pragma unroll
+                for (int ax = 0; ax < 3; ax++) gXm[b] += gpic2[ax] * dpic2[ax][b];
+            scatter_faces(a, P, qm, W2, gpic2, nullptr);
+            #pragma unroll
+            for (int b = 0; b < 3; b++) {
+                gX[b] += gXm[b];
+                gk1[b] = gXm[b] * P.half_dt;
+            }
+            clamp_bwd(c1, pic, gk1, gpic_k1);
+        }
+        float gnvc[3];
+        #pragma unroll
         for (int b = 0; b < 3; b++) {
-            // clamped component: position pinned to the wall, velocity zeroed
-            gX[b] = wall[b] ? 0.0f : gnp[b];
-            gnv[b] = wall[b] ? 0.0f : gnp[b] * dt + gnv_out[b];
+            gnvc[b] = gnv[b] * ff[b];
+#pragma unroll
+            #pragma unroll
+            for (int c = 0; c < 3; c++)
+                if (fsel[b] == c) gX[c] += gnv[b] * nvc[b] * (-friction) * dnr[c];
         }
         float gmix[3];
-        if (clamped) {  // nv = mix * maxs/|mix|
-            const float inv = 1.0f / sp;
-            const float dotp = (gnv[0] * mix[0] + gnv[1] * mix[1] + gnv[2] * mix[2]) * inv * inv;
-            for (int b = 0; b < 3; b++) gmix[b] = sc * (gnv[b] - mix[b] * dotp);
-        } else {
-            for (int b = 0; b < 3; b++) gmix[b] = gnv[b];
-        }
+        clamp_bwd(cm, mix, gnvc, gmix);
         // mix = pic + alpha*(pv - saved)
         float gpv[3], gpic[3], gsv[3];
+        #pragma unroll
         for (int b = 0; b < 3; b++) {
-            gpic[b] = gmix[b];
+            gpic[b] = gmix[b] + gpic_k1[b];
             gpv[b] = alpha * gmix[b];
             gsv[b] = -alpha * gmix[b];
         }
+        #pragma unroll
         for (int b = 0; b < 3; b++)
+            #pragma unroll
             for (int ax = 0; ax < 3; ax++) gX[b] += gpic[ax] * dpic[ax][b] + gsv[ax] * dsv[ax][b];
-        // face gradients: pic_ax = sum (w/W) fin_f, saved likewise
-        for (int ax = 0; ax < 3; ax++) {
-            if (!(W[ax] > 0.0f)) continue;
-            const float cf = gpic[ax] / W[ax], cs = gsv[ax] / W[ax];
-            if (cf == 0.0f && cs == 0.0f) continue;
-            float2* gfs = a.g_fs[ax];
-            stencil(P, ax, q, true, [&](size_t idx, float w, const float*) {
-                atomicAdd(gfs + idx, make_float2(w * cf, w * cs));
-            });
-        }
+        scatter_faces(a, P, q, W, gpic, gsv);
         a.g_sorted[2 * (size_t)d] = make_float4(gX[0], gX[1], gX[2], 0.0f);
         a.g_sorted[2 * (size_t)d + 1] = make_float4(gpv[0], gpv[1], gpv[2], 0.0f);
     }

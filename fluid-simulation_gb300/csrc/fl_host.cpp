@@ -1280,8 +1280,6 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     if (!h || !t || t->h != h) return set_err(h, FL_INVALID_ARG, "tape does not belong to this handle");
     if (t->count == 0) return set_err(h, FL_INVALID_ARG, "tape is empty");
     if (h->n && (!dL_dout_dev || !dL_din_dev)) return set_err(h, FL_INVALID_ARG, "gradient buffer is NULL");
-    if (h->prm.advect_order == 2u || h->prm.phys[3] != 0.0f)
-        return set_err(h, FL_INVALID_ARG, "the adjoint supports advect_order 1 and wall_friction 0");
     const uint32_t k = t->count - 1;
     char* slot = t->slots + (size_t)k * t->slot_bytes;
     cudaStream_t st = h->stream;

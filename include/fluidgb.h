@@ -226,8 +226,10 @@ fl_status fl_load_state_device(fl_handle* h, const void* src_dev, size_t size);
  * the pressure solve is differentiated as an exact solve, so the adjoint runs
  * a second CG with the same operator, the handle's cg_precision and the
  * tape's adjoint solver (fl_tape_set_adjoint_solver), to `adj_cg_tol`
- * relative residual or `adj_cg_iters` iterations.  Requires advect_order 1
- * and wall_friction 0.  Gradient buffers are device pointers.
+ * relative residual or `adj_cg_iters` iterations.  Both advection orders and
+ * the wall-friction band are differentiated (the friction band's min/max
+ * selections and the speed and wall clamps held at the recorded step's
+ * choices).  Gradient buffers are device pointers.
  * fl_tape_last_stats: cg_iterations, rs_initial/rs_final and device_status of
  * the last adjoint pressure solve. */
 typedef struct fl_tape fl_tape;

@@ -10,15 +10,18 @@ compared with central finite differences, eps 1e-3, of the FP64 oracle forward
 its drift term is a function of integer particle counts, held fixed by the
 adjoint.
 
-Runs only with FL_GRADCHECK64=1 (33 FP64 rollouts of 60 substeps take
-minutes on the host cores); prints every direction, and with FL_GRADCHECK_OUT
-writes them as JSON.  FL_GC_STEPS and FL_GC_EPS change the horizon and the
-step (defaults 60 and 1e-3, the configuration's).  The adjoint holds the
-discrete choices of the recorded forward fixed (bins, cell types, clamps); a
-direction whose +-eps runs change cell types sees those jumps in the finite
-difference, so each direction reports how many cell types differ from the
-unperturbed run, and a 1e-2 bound on the median error is asserted over the
-directions that change none.
+Two horizons.  The default suite runs 3 substeps at eps 1e-6: there every
+direction's +-eps runs keep the unperturbed run's cell types (at least 12 of
+16 are required) and the median relative error over them must be at most
+1e-3.  The configuration's own horizon and step (60 substeps, eps 1e-3) run
+with FL_GRADCHECK64=1 (33 FP64 rollouts of 60 substeps take minutes on the
+host cores) and are reported: at that horizon nearly every direction flips
+cell types.  FL_GC_STEPS and FL_GC_EPS override the opt-in run's horizon and
+step; every direction is printed, and with FL_GRADCHECK_OUT written as JSON.
+The adjoint holds the discrete choices of the recorded forward fixed (bins,
+cell types, clamps); a direction whose +-eps runs change cell types sees those
+jumps in the finite difference, so each direction reports how many cell types
+differ from the unperturbed run.
 """
 import json
 import os
@@ -32,12 +35,13 @@ pytestmark = pytest.mark.gpu
 
 TARGET = np.array([0.7, 0.2, 0.5])
 EVERY, DIRECTIONS = 10, 16
+OPT_IN = os.environ.get("FL_GRADCHECK64") == "1"
 # the configuration's horizon and step size; FL_GC_STEPS / FL_GC_EPS vary them
-STEPS = int(os.environ.get("FL_GC_STEPS", "60"))
-EPS = float(os.environ.get("FL_GC_EPS", "1e-3"))
+CONFIG_STEPS = int(os.environ.get("FL_GC_STEPS", "60"))
+CONFIG_EPS = float(os.environ.get("FL_GC_EPS", "1e-3"))
 
 
-def forward_fp64(oracle, p, parts, dv, eps, grav):
+def forward_fp64(oracle, p, parts, dv, eps, grav, steps):
     q = p.copy()
     q.dims[2] = 3000
     q.pressure_tolerance = 1e-9
@@ -47,7 +51,7 @@ def forward_fp64(oracle, p, parts, dv, eps, grav):
     if dv is not None:
         o.add_velocity_d(dv, eps)
     cts = []
-    for _ in range(STEPS):
+    for _ in range(steps):
         o.step(1)
         cts.append(o.get_grid()["cell_type"].copy())
     c = o.mean_position_d()
@@ -55,8 +59,11 @@ def forward_fp64(oracle, p, parts, dv, eps, grav):
     return float(((c - TARGET) ** 2).sum()), np.stack(cts)
 
 
-@pytest.mark.skipif(os.environ.get("FL_GRADCHECK64") != "1", reason="minutes of FP64 host rollouts: FL_GRADCHECK64=1")
-def test_block64_rollout_gradients_against_fp64_finite_differences(oracle):
+@pytest.mark.parametrize("horizon", [
+    "short", pytest.param("configuration", marks=pytest.mark.skipif(
+        not OPT_IN, reason="minutes of FP64 host rollouts: FL_GRADCHECK64=1"))])
+def test_block64_rollout_gradients_against_fp64_finite_differences(oracle, horizon):
+    STEPS, EPS = (3, 1e-6) if horizon == "short" else (CONFIG_STEPS, CONFIG_EPS)
     torch = pytest.importorskip("torch")
     from fluidgb import build
     from fluidgb.autograd import Rollout, RolloutFunction, com_loss
@@ -82,13 +89,13 @@ def test_block64_rollout_gradients_against_fp64_finite_differences(oracle):
     rows = []
     try:
         base_g = np.array([0.0, np.float32(-9.81), 0.0], np.float64)
-        _, ct0 = forward_fp64(oracle, p, parts, None, 0.0, base_g)
+        _, ct0 = forward_fp64(oracle, p, parts, None, 0.0, base_g, STEPS)
         rng = np.random.default_rng(4)
         for k in range(DIRECTIONS):
             dv = rng.standard_normal((n, 3))
             dg = rng.standard_normal(3)
-            lp, ctp = forward_fp64(oracle, p, parts, dv, EPS, base_g + EPS * dg)
-            lm, ctm = forward_fp64(oracle, p, parts, dv, -EPS, base_g - EPS * dg)
+            lp, ctp = forward_fp64(oracle, p, parts, dv, EPS, base_g + EPS * dg, STEPS)
+            lm, ctm = forward_fp64(oracle, p, parts, dv, -EPS, base_g - EPS * dg, STEPS)
             fd = (lp - lm) / (2 * EPS)
             ad = float((gv * dv).sum() + (gg * dg).sum())
             rel = abs(ad - fd) / max(abs(fd), 1e-12)
@@ -111,5 +118,8 @@ def test_block64_rollout_gradients_against_fp64_finite_differences(oracle):
     # +-eps runs take the same discrete branch; on those directions the median
     # error is bounded (the f32 forward's rounding, amplified along the
     # horizon, sets the rest).
-    if smooth:
+    if horizon == "short":
+        assert len(smooth) >= 12, rows
+        assert np.median(smooth) <= 1e-3, smooth
+    elif smooth:
         assert np.median(smooth) < 1e-2, smooth

@@ -13,19 +13,24 @@
 //
 //   k_adj_g2p       g2p.wgsl:131-198 (friction band, speed clamp, forward Euler
 //                   or the midpoint step, wall clamp): particle gradients
-//                   w.r.t. position and velocity, and face gradients of the
-//                   final and saved velocities (scatter = transpose of the
-//                   trilinear gather; one float2 vector atomic per tap into
-//                   the interleaved {final, saved} gradients)
+//                   w.r.t. position and velocity, and per particle the face
+//                   coefficients of its gathers (gradient / weight sum)
+//   k_adj_mid       (midpoint step) the midpoint gather's face gradients as
+//                   64-bit fixed-point integer atomics (order-free)
+//   k_adj_gather    per face, in a fixed order over the particles of the
+//                   cells around it: the face gradients of the final and
+//                   saved velocities (the trilinear gather transposed) and
+//                   scatter.wgsl's sums {sum w, sum w v} without the
+//                   fixed-point rounding.  No float atomics anywhere: two
+//                   backward passes give the same bits
 //   k_adj_prhs      gradient.wgsl transposed: dL/dp per liquid cell, the RHS
 //                   of the adjoint pressure solve A lambda = dL/dp
 //   k_adj_thr       (warm start only) the solve's absolute stopping threshold
 //   (k_solve_init + k_cg with the RHS: the adjoint solve)
 //   k_adj_faces     divergence.wgsl and gradient.wgsl transposed, then
 //                   boundaries.wgsl / forces.wgsl / save_vel.wgsl: gradient of
-//                   the normalised P2G face velocity, and dL/dgravity
-//   k_adj_p2g_sums  scatter.wgsl without the fixed-point rounding: {sum w,
-//                   sum w v} per face (one float2 vector atomic per tap)
+//                   the normalised P2G face velocity; dL/dgravity as block
+//                   partials, summed in order by k_adj_grav
 //   k_adj_p2g       scatter.wgsl transposed: a gather from faces to particles
 //                   (velocity and position gradients)
 //   k_adj_unsort    sort_scatter.wgsl transposed: back to the step's input order
@@ -180,21 +185,6 @@ __device__ __forceinline__ void clamp_bwd(const Clamp& c, const float v[3], cons
     }
 }
 
-// Face gradients of a wall-aware gather at q: d(sum w f / W)/d f = w/W.
-__device__ __forceinline__ void scatter_faces(const AdjBufs& a, const DevParams& P, const float q[3], const float W[3],
-                                              const float gfin[3], const float gsav[3]) {
-    #pragma unroll
-    for (int ax = 0; ax < 3; ax++) {
-        if (!(W[ax] > 0.0f)) continue;
-        const float cf = gfin[ax] / W[ax], cs = gsav ? gsav[ax] / W[ax] : 0.0f;
-        if (cf == 0.0f && cs == 0.0f) continue;
-        float2* gfs = a.g_fs[ax];
-        stencil(P, ax, q, true, [&](size_t idx, float w, const float*) {
-            atomicAdd(gfs + idx, make_float2(w * cf, w * cs));
-        });
-    }
-}
-
 // g2p.wgsl:131-198 and the midpoint option, in reverse.  Forward recomputed
 // per particle: PIC and saved gathers at X, mix, speed clamp, the friction
 // band factors (g2p.wgsl:173-184), then forward Euler (g2p.wgsl:186) or the
@@ -291,7 +281,14 @@ __global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
             for (int b = 0; b < 3; b++)
                 #pragma unroll
                 for (int ax = 0; ax < 3; ax++) gXm[b] += gpic2[ax] * dpic2[ax][b];
-            scatter_faces(a, P, qm, W2, gpic2, nullptr);
+            // midpoint-stencil coefficients: gfin/W2 per axis, scattered by k_adj_mid
+            float c2[3];
+#pragma unroll
+            for (int ax = 0; ax < 3; ax++) c2[ax] = W2[ax] > 0.0f ? gpic2[ax] / W2[ax] : 0.0f;
+            a.mid[2 * (size_t)d] = make_float4(qm[0], qm[1], qm[2], 0.0f);
+            a.mid[2 * (size_t)d + 1] = make_float4(c2[0], c2[1], c2[2], 0.0f);
+            const float m2 = fmaxf(fmaxf(fabsf(c2[0]), fabsf(c2[1])), fabsf(c2[2]));
+            if (m2 > 0.0f) atomicMax(&a.flags[1], __float_as_uint(m2));  // order-free
             #pragma unroll
             for (int b = 0; b < 3; b++) {
                 gX[b] += gXm[b];
@@ -322,7 +319,17 @@ __global__ void __launch_bounds__(256) k_adj_g2p(AdjBufs a) {
         for (int b = 0; b < 3; b++)
             #pragma unroll
             for (int ax = 0; ax < 3; ax++) gX[b] += gpic[ax] * dpic[ax][b] + gsv[ax] * dsv[ax][b];
-        scatter_faces(a, P, q, W, gpic, gsv);
+        // face coefficients of the gathers at X, summed per face by k_adj_gather
+        float cf[3], cs[3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ax++) {
+            cf[ax] = W[ax] > 0.0f ? gpic[ax] / W[ax] : 0.0f;
+            cs[ax] = W[ax] > 0.0f ? gsv[ax] / W[ax] : 0.0f;
+        }
+        a.coef[3 * (size_t)d] = make_float4(q[0], q[1], q[2], pv[0]);
+        a.coef[3 * (size_t)d + 1] = make_float4(pv[1], pv[2], cf[0], cf[1]);
+        a.coef[3 * (size_t)d + 2] = make_float4(cf[2], cs[0], cs[1], cs[2]);
+        if (pos.w != 0.0f) a.flags[0] = 1u;  // a stray particle (its P2G cell is not its bin)
         a.g_sorted[2 * (size_t)d] = make_float4(gX[0], gX[1], gX[2], 0.0f);
         a.g_sorted[2 * (size_t)d + 1] = make_float4(gpv[0], gpv[1], gpv[2], 0.0f);
     }
@@ -429,7 +436,8 @@ __global__ void __launch_bounds__(256) k_adj_faces(AdjBufs a, int axis) {
         }
         a.g_norm[axis][f] = gpre + a.g_fs[axis][f].y;
     }
-    // dL/dg_axis (fixed order within the block, atomics across blocks)
+    // dL/dg_axis: the block's partial in a fixed order (k_adj_grav sums the
+    // blocks' partials in order)
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gg += __shfl_down_sync(0xffffffffu, gg, o);
     if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = gg;
@@ -437,31 +445,176 @@ __global__ void __launch_bounds__(256) k_adj_faces(AdjBufs a, int axis) {
     if (threadIdx.x == 0) {
         double s = 0.0;
         for (int w = 0; w < 8; w++) s += s_red[w];
-        if (s != 0.0) atomicAdd(&a.g_grav[axis], s);
+        a.grav_part[axis][blockIdx.x] = s;
     }
 }
 
-// P2G transposed: vel_f = sum_p w v / sum_p w  ->  gather per particle.
-// scatter.wgsl's sums without the fixed-point rounding: the point at which
-// k_adj_p2g linearises the normalisation.  Bin order keeps the atomics of a
-// warp on neighbouring faces.
-__global__ void __launch_bounds__(256) k_adj_p2g_sums(AdjBufs a) {
+// dL/dgravity: per axis (one block each) the k_adj_faces partials, thread t
+// summing partials t, t + 1024, ... in sequence, then a fixed tree.
+__global__ void __launch_bounds__(1024) k_adj_grav(AdjBufs a, uint32_t nb0, uint32_t nb1, uint32_t nb2) {
+    __shared__ double s_red[32];
+    const uint32_t axis = blockIdx.x, nb = axis == 0 ? nb0 : (axis == 1 ? nb1 : nb2);
+    const double* part = a.grav_part[axis];
+    double s = 0.0;
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x) s += part[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = s_red[threadIdx.x];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) a.g_grav[axis] = v;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Face gradients and P2G sums, gathered per face in a fixed order.
+
+// Scale of the midpoint stencil's 64-bit fixed-point sums: with m the largest
+// |coefficient| of the step (flags[1]), m < 2^e, and at most 2^24 terms per
+// face, |sum| * 2^(38 - e) < 2^62.  Quantum about 7e-12 m.
+__device__ __forceinline__ int mid_exponent(const AdjBufs& a) {
+    const float m = __uint_as_float(a.flags[1]);
+    int e = 0;
+    frexpf(m, &e);
+    return 38 - e;
+}
+
+// The midpoint step's face gradients: each particle's wall-aware stencil at
+// its midpoint Xm, w * (gfin/W at Xm), added as 64-bit fixed-point integers
+// (integer sums do not depend on the order of the atomics).
+__global__ void __launch_bounds__(256) k_adj_mid(AdjBufs a) {
     const DevParams& P = *a.prm;
     const uint32_t n = P.n;
-    const float inv_h = P.inv_h;
+    if (a.flags[1] == 0u) return;
+    const double scale = ldexp(1.0, mid_exponent(a));
     for (uint32_t d = blockIdx.x * blockDim.x + threadIdx.x; d < n; d += gridDim.x * blockDim.x) {
-        const float4 pos = a.part[2 * (size_t)d], pvel = a.part[2 * (size_t)d + 1];
-        const float q[3] = {(pos.x - P.origin[0]) * inv_h, (pos.y - P.origin[1]) * inv_h, (pos.z - P.origin[2]) * inv_h};
-        const float pv[3] = {pvel.x, pvel.y, pvel.z};
+        const float4 qm4 = a.mid[2 * (size_t)d], c4 = a.mid[2 * (size_t)d + 1];
+        const float qm[3] = {qm4.x, qm4.y, qm4.z}, c2[3] = {c4.x, c4.y, c4.z};
+#pragma unroll
         for (int ax = 0; ax < 3; ax++) {
-            float2* ws = a.wsum[ax];
-            stencil(P, ax, q, false, [&](size_t idx, float w, const float*) {
-                atomicAdd(ws + idx, make_float2(w, w * pv[ax]));
+            if (c2[ax] == 0.0f) continue;
+            unsigned long long* g = a.gmid[ax];
+            stencil(P, ax, qm, true, [&](size_t idx, float w, const float*) {
+                atomicAdd(g + idx, (unsigned long long)llrint((double)(w * c2[ax]) * scale));
             });
         }
     }
 }
 
+// One thread per cell (i, j, k): the low faces u(i,j,k), v(i,j,k), w(i,j,k)
+// of the cell, and on the grid's high sides also u(nx,j,k), v(i,ny,k),
+// w(i,j,nz).  Every particle whose trilinear stencil (at its cell-space
+// position q, scatter.wgsl:44-117 / g2p.wgsl:56-129) reaches one of these
+// faces lies in the cells i-1..i+1, j-1..j+1, k-1..k+1 (two cells on every
+// side when the step has stray particles, whose P2G cell differs from their
+// bin by one); each (y, z) row of them is one contiguous range of the
+// bin-ordered particles.  The rows are visited in (z, y) order and their
+// particles in bin order, so every face's sums come out the same on every run:
+//   g_fs = {sum w gpic/W, sum w gsaved/W}  (0 on faces touching the static
+//          walls, which the wall-aware gathers skip) + the midpoint stencil's sum,
+//   wsum = {sum w, sum w v_axis}  (every in-range tap, like scatter.wgsl).
+// Candidates read the compact record {q, v_x} (16 B); the rest of a
+// particle's record only when it has a tap among the faces.
+__global__ void __launch_bounds__(256) k_adj_gather(AdjBufs a, int midpoint) {
+    const DevParams& P = *a.prm;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.C) return;
+    const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
+    const int i = (int)(c % (uint32_t)nx), j = (int)((c / (uint32_t)nx) % (uint32_t)ny), k = (int)(c / ((uint32_t)nx * ny));
+    const int cc[3] = {i, j, k}, n3[3] = {nx, ny, nz};
+    // faces: 0..2 the low faces of axis 0..2, 3..5 the high-side faces of axis 0..2
+    bool has[6];
+    int fc[6][3];
+    bool wall[6];
+#pragma unroll
+    for (int e = 0; e < 6; e++) {
+        const int ax = e % 3;
+#pragma unroll
+        for (int b = 0; b < 3; b++) fc[e][b] = cc[b] + (e >= 3 && b == ax ? 1 : 0);
+        has[e] = e < 3 || cc[ax] == n3[ax] - 1;
+        wall[e] = touches_static_a(ax, fc[e][0], fc[e][1], fc[e][2], nx, ny, nz);
+    }
+    const int rad = a.flags[0] ? 2 : 1;
+    int lo[3], hi[3];
+#pragma unroll
+    for (int b = 0; b < 3; b++) {
+        lo[b] = max(cc[b] - rad, 0);
+        hi[b] = min(cc[b] + rad, n3[b] - 1);
+    }
+    const uint32_t n = P.n, C = P.C;
+    float gf[6], gs[6], W[6], WV[6];
+#pragma unroll
+    for (int e = 0; e < 6; e++) gf[e] = gs[e] = W[e] = WV[e] = 0.0f;
+    for (int ck = lo[2]; ck <= hi[2]; ck++) {
+        for (int cj = lo[1]; cj <= hi[1]; cj++) {
+            const uint32_t row = (uint32_t)nx * ((uint32_t)cj + (uint32_t)ny * (uint32_t)ck);
+            const uint32_t d0 = a.cell_first[row + lo[0]];
+            const uint32_t e1 = row + (uint32_t)hi[0] + 1u;
+            const uint32_t d1 = e1 < C ? a.cell_first[e1] : n;
+            for (uint32_t d = d0; d < d1; d++) {
+                const float4 r0 = a.coef[3 * (size_t)d];
+                const float q[3] = {r0.x, r0.y, r0.z};
+                // per dimension, the stencil's weight for face coordinate cc (lo) and
+                // cc + 1 (hi) along the face axis (g = q + 0), and for cc across it
+                // (g = q - 0.5); 0 where the coordinate is not one of the two taps
+                float wlo[3], whi[3], wx[3];
+#pragma unroll
+                for (int b = 0; b < 3; b++) {
+                    const float g0 = q[b] + 0.0f, g1 = q[b] + -0.5f;
+                    const int b0 = __float2int_rz(floorf(g0)), b1 = __float2int_rz(floorf(g1));
+                    const float t0 = g0 - (float)b0, t1 = g1 - (float)b1;
+                    const int o0 = cc[b] - b0, o1 = cc[b] - b1;
+                    wlo[b] = o0 == 0 ? 1.0f - t0 : (o0 == 1 ? t0 : 0.0f);
+                    whi[b] = o0 == -1 ? 1.0f - t0 : (o0 == 0 ? t0 : 0.0f);
+                    wx[b] = o1 == 0 ? 1.0f - t1 : (o1 == 1 ? t1 : 0.0f);
+                }
+                float w[6];
+                bool any = false;
+#pragma unroll
+                for (int e = 0; e < 6; e++) {
+                    const int ax = e % 3;
+                    const float f0 = ax == 0 ? (e >= 3 ? whi[0] : wlo[0]) : wx[0];
+                    const float f1 = ax == 1 ? (e >= 3 ? whi[1] : wlo[1]) : wx[1];
+                    const float f2 = ax == 2 ? (e >= 3 ? whi[2] : wlo[2]) : wx[2];
+                    w[e] = has[e] ? f0 * f1 * f2 : 0.0f;  // (wx * wy) * wz, the stencil's order
+                    any = any || w[e] != 0.0f;
+                }
+                if (!any) continue;
+                const float4 r1 = a.coef[3 * (size_t)d + 1], r2 = a.coef[3 * (size_t)d + 2];
+                const float v[3] = {r0.w, r1.x, r1.y}, cf[3] = {r1.z, r1.w, r2.x}, cs[3] = {r2.y, r2.z, r2.w};
+#pragma unroll
+                for (int e = 0; e < 6; e++) {
+                    const int ax = e % 3;
+                    if (w[e] == 0.0f) continue;  // not a tap (a tap of weight 0 adds nothing either)
+                    W[e] += w[e];
+                    WV[e] += w[e] * v[ax];
+                    if (!wall[e]) {
+                        gf[e] += w[e] * cf[ax];
+                        gs[e] += w[e] * cs[ax];
+                    }
+                }
+            }
+        }
+    }
+    const double mscale = midpoint && a.flags[1] != 0u ? ldexp(1.0, -mid_exponent(a)) : 0.0;
+#pragma unroll
+    for (int e = 0; e < 6; e++) {
+        if (!has[e]) continue;
+        const int ax = e % 3;
+        const uint32_t dxa = (uint32_t)nx + (ax == 0), dya = (uint32_t)ny + (ax == 1);
+        const size_t f = (size_t)fc[e][0] + dxa * ((size_t)fc[e][1] + (size_t)dya * fc[e][2]);
+        float g = gf[e];
+        if (mscale != 0.0 && !wall[e]) g += (float)((double)(long long)a.gmid[ax][f] * mscale);
+        a.g_fs[ax][f] = make_float2(g, gs[e]);
+        a.wsum[ax][f] = make_float2(W[e], WV[e]);
+    }
+}
+
+// P2G transposed: vel_f = sum_p w v / sum_p w  ->  gather per particle, with
+// the normalisation linearised at the unquantised sums k_adj_gather wrote.
 __global__ void __launch_bounds__(256) k_adj_p2g(AdjBufs a) {
     const DevParams& P = *a.prm;
     const uint32_t n = P.n;
@@ -515,10 +668,15 @@ cudaError_t launch_adj_thr(const AdjBufs& a, uint32_t nchunks, double tol_sq, De
 }
 cudaError_t launch_adj_faces(const AdjBufs& a, const uint32_t F3[3], cudaStream_t s) {
     for (int ax = 0; ax < 3; ax++) k_adj_faces<<<(F3[ax] + 255) / 256, 256, 0, s>>>(a, ax);
+    k_adj_grav<<<3, 1024, 0, s>>>(a, (F3[0] + 255) / 256, (F3[1] + 255) / 256, (F3[2] + 255) / 256);
     return cudaGetLastError();
 }
-cudaError_t launch_adj_p2g_sums(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {
-    k_adj_p2g_sums<<<L.particle_blocks, 256, 0, s>>>(a);
+cudaError_t launch_adj_mid(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {
+    k_adj_mid<<<L.particle_blocks, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+cudaError_t launch_adj_gather(const AdjBufs& a, uint32_t C, bool midpoint, cudaStream_t s) {
+    k_adj_gather<<<(C + 255) / 256, 256, 0, s>>>(a, midpoint ? 1 : 0);
     return cudaGetLastError();
 }
 cudaError_t launch_adj_p2g(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s) {

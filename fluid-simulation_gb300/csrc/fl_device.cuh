@@ -133,13 +133,20 @@ struct AdjBufs {
     float4* g_in;            // dL/d(input particle), input order
     float2* g_fs[3];         // {dL/d final face velocity, dL/d saved face velocity} per face
     float* g_norm[3];
-    // Unquantised P2G sums {sum w, sum w v} of the recorded step (scratch that
-    // aliases g_fs once k_adj_faces has consumed it).
+    // Unquantised P2G sums {sum w, sum w v} of the recorded step.
     float2* wsum[3];
     float* lam;              // adjoint pressure (the solve's x)
     float* rhs;              // dL/dp
     float2* rhs_part;        // per-chunk float-float partials of rhs.rhs (null: not needed)
-    double* g_grav;          // 3 accumulators
+    double* g_grav;          // 3 sums of the block partials
+    double* grav_part[3];    // per k_adj_faces block: its partial of dL/dgravity
+    // Deterministic face gradients (gathered per face in a fixed order).
+    float4* coef;            // per particle (bin order), 3 float4: {q, v_x}, {v_y, v_z, gpic_x/W, gpic_y/W},
+                             // {gpic_z/W, gsaved/W per axis}
+    const uint32_t* cell_first;  // first bin-ordered particle of every cell (the step's bin offsets)
+    uint32_t* flags;         // [0] the step has stray particles, [1] max |midpoint coefficient| (float bits)
+    float4* mid;             // midpoint step: per particle {qm.xyz, _}, {gfin/W at qm per axis, _}
+    unsigned long long* gmid[3];  // midpoint-stencil face gradients, 64-bit fixed point
 };
 
 // ---------------------------------------------------------------------------
@@ -351,7 +358,10 @@ cudaError_t launch_adj_prhs(const AdjBufs& a, uint32_t C, cudaStream_t s);
 // tol^2 * (rhs.rhs) into cg_prm's absolute threshold (rhs_part of a block-per-chunk k_adj_prhs)
 cudaError_t launch_adj_thr(const AdjBufs& a, uint32_t nchunks, double tol_sq, DevParams* cg_prm, cudaStream_t s);
 cudaError_t launch_adj_faces(const AdjBufs& a, const uint32_t F3[3], cudaStream_t s);
-cudaError_t launch_adj_p2g_sums(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
+// the midpoint step's face gradients into gmid (zeroed by the caller)
+cudaError_t launch_adj_mid(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
+// g_fs and wsum of every face, gathered per cell in a fixed order
+cudaError_t launch_adj_gather(const AdjBufs& a, uint32_t C, bool midpoint, cudaStream_t s);
 cudaError_t launch_adj_p2g(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_adj_unsort(const AdjBufs& a, const LaunchCfg& L, cudaStream_t s);
 // Stand-alone CG on prepared cell arrays (used by fl_solve_pressure).

@@ -1086,10 +1086,16 @@ struct fl_tape {
     uint32_t max_steps = 0, count = 0;
     void* pool = nullptr;
     char* slots = nullptr;
-    size_t slot_bytes = 0, o_part = 0, o_perm = 0, o_ct = 0, o_sav[3] = {}, o_fin[3] = {};
+    size_t slot_bytes = 0, o_part = 0, o_perm = 0, o_ct = 0, o_off = 0, o_sav[3] = {}, o_fin[3] = {};
     float4* g_sorted = nullptr;
     float2* g_fs[3] = {};
     float* g_norm[3] = {};
+    float2* wsum[3] = {};
+    unsigned long long* gmid[3] = {};
+    double* grav_part[3] = {};
+    float4* coef = nullptr;
+    float4* mid = nullptr;
+    uint32_t* flags = nullptr;
     float* rhs = nullptr;
     double* g_grav = nullptr;
     DevBufs cg{};        // buffers of the adjoint pressure solve (cg.p holds lambda)
@@ -1116,6 +1122,7 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     t->o_part = slot.take<float4>(2 * cap);
     t->o_perm = slot.take<uint32_t>(cap);
     t->o_ct = slot.take<uint8_t>(C);
+    t->o_off = slot.take<uint32_t>(C);  // the step's bin offsets (first particle of every cell)
     for (int a = 0; a < 3; a++) {
         t->o_sav[a] = slot.take<float>(h->F3[a]);
         t->o_fin[a] = slot.take<float>(h->F3[a]);
@@ -1123,11 +1130,15 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     t->slot_bytes = (slot.off + 255) & ~size_t(255);
     PoolPlan pl;
     pl.off = t->slot_bytes * max_steps;
-    size_t o_gs = pl.take<float4>(2 * cap), o_gf[3], o_gn[3];
+    size_t o_gs = pl.take<float4>(2 * cap), o_gf[3], o_gn[3], o_ws[3], o_gm[3], o_gp[3];
     for (int a = 0; a < 3; a++) {
         o_gf[a] = pl.take<float2>(h->F3[a]);
         o_gn[a] = pl.take<float>(h->F3[a]);
+        o_ws[a] = pl.take<float2>(h->F3[a]);
+        o_gm[a] = pl.take<unsigned long long>(h->F3[a]);
+        o_gp[a] = pl.take<double>((h->F3[a] + 255) / 256);
     }
+    const size_t o_coef = pl.take<float4>(3 * cap), o_mid = pl.take<float4>(2 * cap), o_flags = pl.take<uint32_t>(2);
     size_t o_rhs = pl.take<float>(C), o_lam = pl.take<float>(C), o_r = pl.take<float>(C), o_dA = pl.take<float>(C),
            o_dB = pl.take<float>(C), o_q = pl.take<float>(C), o_ci = pl.take<uint16_t>(C), o_fl = pl.take<uint8_t>(nch),
            o_prr = pl.take<float>(nch), o_c64 = pl.take<float2>(nch), o_plan = pl.take<uint32_t>(nch),
@@ -1147,7 +1158,13 @@ fl_status fl_tape_create(fl_handle* h, uint32_t max_steps, fl_tape** out) {
     for (int a = 0; a < 3; a++) {
         t->g_fs[a] = (float2*)(base + o_gf[a]);
         t->g_norm[a] = (float*)(base + o_gn[a]);
+        t->wsum[a] = (float2*)(base + o_ws[a]);
+        t->gmid[a] = (unsigned long long*)(base + o_gm[a]);
+        t->grav_part[a] = (double*)(base + o_gp[a]);
     }
+    t->coef = (float4*)(base + o_coef);
+    t->mid = (float4*)(base + o_mid);
+    t->flags = (uint32_t*)(base + o_flags);
     t->rhs = (float*)(base + o_rhs);
     t->g_grav = (double*)(base + o_gg);
     DevBufs& b = t->cg;
@@ -1235,6 +1252,7 @@ fl_status tape_append(fl_handle* h, fl_tape* t) {
         FL_CUDA(h, cudaMemcpyAsync(slot + t->o_perm, h->b.perm, 4 * n, cudaMemcpyDeviceToDevice, st));
     }
     FL_CUDA(h, cudaMemcpyAsync(slot + t->o_ct, h->b.ct, h->C, cudaMemcpyDeviceToDevice, st));
+    FL_CUDA(h, cudaMemcpyAsync(slot + t->o_off, h->b.offsets, 4 * (size_t)h->C, cudaMemcpyDeviceToDevice, st));
     for (int a = 0; a < 3; a++) {
         const size_t fb = 4 * (size_t)h->F3[a];
         FL_CUDA(h, cudaMemcpyAsync(slot + t->o_sav[a], h->b.sav[a], fb, cudaMemcpyDeviceToDevice, st));
@@ -1288,14 +1306,22 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     a.part = (const float4*)(slot + t->o_part);
     a.perm = (const uint32_t*)(slot + t->o_perm);
     a.ct = (const uint8_t*)(slot + t->o_ct);
+    a.cell_first = (const uint32_t*)(slot + t->o_off);
+    const bool midpoint = h->prm.advect_order == 2u;
     for (int ax = 0; ax < 3; ax++) {
         a.sav[ax] = (const float*)(slot + t->o_sav[ax]);
         a.fin[ax] = (const float*)(slot + t->o_fin[ax]);
         a.g_fs[ax] = t->g_fs[ax];
         a.g_norm[ax] = t->g_norm[ax];
-        a.wsum[ax] = t->g_fs[ax];  // free once k_adj_faces has run
-        FL_CUDA(h, cudaMemsetAsync(t->g_fs[ax], 0, sizeof(float2) * (size_t)h->F3[ax], st));
+        a.wsum[ax] = t->wsum[ax];
+        a.gmid[ax] = t->gmid[ax];
+        a.grav_part[ax] = t->grav_part[ax];
+        if (midpoint) FL_CUDA(h, cudaMemsetAsync(t->gmid[ax], 0, 8 * (size_t)h->F3[ax], st));
     }
+    a.coef = t->coef;
+    a.mid = t->mid;
+    a.flags = t->flags;
+    FL_CUDA(h, cudaMemsetAsync(t->flags, 0, 2 * sizeof(uint32_t), st));
     a.g_out = (const float4*)dL_dout_dev;
     a.g_sorted = t->g_sorted;
     a.g_in = (float4*)dL_din_dev;
@@ -1303,8 +1329,9 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
     a.rhs = t->rhs;
     a.rhs_part = t->adj_warm ? t->cg.chunk_rr_df : nullptr;  // free until k_solve_init
     a.g_grav = t->g_grav;
-    FL_CUDA(h, cudaMemsetAsync(t->g_grav, 0, 3 * sizeof(double), st));
     FL_CUDA(h, fl::launch_adj_g2p(a, h->L, st));
+    if (midpoint) FL_CUDA(h, fl::launch_adj_mid(a, h->L, st));
+    FL_CUDA(h, fl::launch_adj_gather(a, h->C, midpoint, st));
     FL_CUDA(h, fl::launch_adj_prhs(a, h->C, st));
     // adjoint pressure solve: A lambda = dL/dp (k_solve_init's rhs is
     // -scale*div, so scale = -1 passes dL/dp through unchanged).  Cold start:
@@ -1338,10 +1365,6 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
         FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
     }
     FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));
-    for (int ax = 0; ax < 3; ax++) {
-        FL_CUDA(h, cudaMemsetAsync(a.wsum[ax], 0, sizeof(float2) * (size_t)h->F3[ax], st));
-    }
-    FL_CUDA(h, fl::launch_adj_p2g_sums(a, h->L, st));
     FL_CUDA(h, fl::launch_adj_p2g(a, h->L, st));
     FL_CUDA(h, fl::launch_adj_unsort(a, h->L, st));
     double gg[3];

@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--adj-solver", choices=["follow", "cg", "mgpcg"], default="mgpcg",
                     help="solver of the adjoint pressure systems (default: the multigrid-preconditioned CG; "
                          "the forward keeps the reference CG unless --adj-mgpcg)")
+    ap.add_argument("--extra-legs", default="block256,dam128",
+                    help="other configurations measured after the headline (comma list; '' = none): "
+                         "forward steps/s, stage rooflines, device memory; block256 also forward+adjoint")
     ap.add_argument("--adj-cold", action="store_true",
                     help="start every adjoint pressure solve from zero (default: from the next step's solution)")
     return ap.parse_args()
@@ -281,6 +284,67 @@ def adjoint_leg(torch, p, parts, steps, every, cg_iters, cg_tol, warm=True, plog
             "device_bytes": used, "device_bytes_note": "handle + tape + checkpoints + torch buffers of the rollout"}
 
 
+def stage_profile(g, n, nx, ny, nz, steps, peak):
+    """Per-stage CUDA-event times over `steps` substeps, and every stage's
+    algorithmic GB/s and fraction of the HBM peak (the byte model above)."""
+    g.set_profiling(True)
+    g.reset_stage_times()
+    liquid_sum = iters_sum = cg_bytes = 0
+    for _ in range(steps):
+        g.step(1)
+        s = g.stats()
+        liquid_sum += s["liquid_cells"]
+        iters_sum += s["cg_iterations"]
+        cg_bytes += algorithmic_bytes("cg", n, nx, ny, nz, s["liquid_cells"], s["cg_iterations"])
+    stage_ms, nprof = g.stage_times()
+    g.set_profiling(False)
+    liquid_avg, iters_avg = liquid_sum / max(nprof, 1), iters_sum / max(nprof, 1)
+    roof = {}
+    for k, ms in stage_ms.items():
+        if ms <= 0.0:
+            continue
+        b = cg_bytes if k == "cg" else algorithmic_bytes(k, n, nx, ny, nz, liquid_avg, iters_avg) * nprof
+        gbs = b / (ms / 1000.0) / 1e9
+        roof[k] = {"algorithmic_gbs": gbs, "frac": gbs / peak}
+    return ({k: v / max(nprof, 1) for k, v in stage_ms.items()}, roof, liquid_avg, iters_avg, cg_bytes, stage_ms,
+            nprof)
+
+
+def extra_leg(torch, name, stream, steps, warmup, profile_steps, adj_steps, adj_every, peak):
+    """Another configuration on the same GPU, after the headline: forward
+    steps/s (CUDA events over `steps` substeps after `warmup`), the stages'
+    rooflines, the handle's device memory, and (adj_steps > 0) the
+    forward+adjoint ratio of a checkpointed rollout."""
+    import fluidgb
+    from fluidgb import scenes
+    p, parts, spec = scenes.workload(name)
+    n = parts.shape[0]
+    nx = spec["n"]
+    free0 = torch.cuda.mem_get_info()[0]
+    g = fluidgb.Fluid(p, n)
+    handle_bytes = free0 - torch.cuda.mem_get_info()[0]
+    g.set_stream(stream.cuda_stream)
+    g.set_particles(parts)
+    g.step(warmup)
+    g.sync()
+    ms = timed_steps(torch, g, steps)
+    st = g.stats()
+    if st["device_status"] != 0:
+        raise RuntimeError("device status %d (%s)" % (st["device_status"], name))
+    stage_ms, roof, liquid_avg, iters_avg, _, _, _ = stage_profile(g, n, nx, nx, nx, profile_steps, peak)
+    g.close()
+    out = {"workload": name, "grid": [nx] * 3, "particles": int(n), "cg_max_iters": spec["iters"],
+           "cg_tol": spec["tol"], "value": steps / (ms / 1000.0), "unit": "steps/s", "ms_per_step": ms / steps,
+           "steps": steps, "warmup": warmup, "window": "substeps %d-%d of the scene" % (warmup + 1, warmup + steps),
+           "stage_ms_per_step": stage_ms, "stage_roofline": roof, "avg_liquid_cells": liquid_avg,
+           "avg_cg_iterations": iters_avg, "handle_device_bytes": handle_bytes}
+    if adj_steps > 0:
+        out["fwd_adjoint"] = adjoint_leg(torch, p, parts, adj_steps, adj_every, spec["iters"], spec["tol"],
+                                         adj_solver=fluidgb.FL_SOLVER_MGPCG)
+        out["fwd_adjoint"]["adjoint_solver"] = "mgpcg"
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -438,6 +502,15 @@ def run_ours(args):
     e2e_value = world * args.e2e_steps / float(tt.item())
     g.close()
 
+    # The other configurations, one after another (rank 0 of a 1-GPU run):
+    # the 256^3 block (forward and forward+adjoint) and the full-depth 128^3
+    # dam break (4.19M particles).
+    legs = {}
+    if rank == 0 and world == 1:
+        for name in [x for x in args.extra_legs.split(",") if x and x != args.workload]:
+            legs[name] = extra_leg(torch, name, stream, 10, 3, 3, 20 if name == "block256" else 0, 10, peak)
+            torch.cuda.set_stream(stream)
+
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.workload, args.cpu_budget, seed)
@@ -465,6 +538,7 @@ def run_ours(args):
             "fp64_reductions": fp64,
             "mgpcg": mg,
             "fwd_adjoint": adj,
+            "configurations": legs or None,
             "cpu_baseline": cb,
             "clocks": clock_rec,
             "gpu_launches": KERNELS_PER_STEP * args.steps,

@@ -333,6 +333,12 @@ def extra_leg(torch, name, stream, steps, warmup, profile_steps, adj_steps, adj_
         raise RuntimeError("device status %d (%s)" % (st["device_status"], name))
     stage_ms, roof, liquid_avg, iters_avg, _, _, _ = stage_profile(g, n, nx, nx, nx, profile_steps, peak)
     g.close()
+    tpath = os.path.join(REPO, "profiles", "traffic.json")  # ncu DRAM bytes per launch, where captured
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            captured = json.load(f).get(name, {})
+        for k in roof:
+            roof[k]["traffic"] = captured.get(k)
     out = {"workload": name, "grid": [nx] * 3, "particles": int(n), "cg_max_iters": spec["iters"],
            "cg_tol": spec["tol"], "value": steps / (ms / 1000.0), "unit": "steps/s", "ms_per_step": ms / steps,
            "steps": steps, "warmup": warmup, "window": "substeps %d-%d of the scene" % (warmup + 1, warmup + steps),

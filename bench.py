@@ -43,7 +43,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default="dam128_2m")
-    ap.add_argument("--precision", choices=["f32", "f64"], default="f32")
+    ap.add_argument("--precision", choices=["f32", "f64", "f64ieee"], default="f32")
     ap.add_argument("--profile-steps", type=int, default=20)
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
@@ -365,7 +365,7 @@ def run_ours(args):
         dist.init_process_group("nccl")
     build.build()
     fluidgb.load_library()
-    prec = fluidgb.FL_CG_F64 if args.precision == "f64" else fluidgb.FL_CG_F32
+    prec = {"f32": fluidgb.FL_CG_F32, "f64": fluidgb.FL_CG_F64, "f64ieee": fluidgb.FL_CG_F64_IEEE}[args.precision]
     seed = scenes.DEFAULT_SEED + rank
     p, parts, spec = scenes.workload(args.workload, seed=seed, precision=prec)
     n = parts.shape[0]
@@ -401,11 +401,11 @@ def run_ours(args):
     ms_max = float(t.item())
     value = replica_value(world, args.steps, ms_max)
 
-    # FP64-reduction variant on the same scene and schedule.
-    fp64 = None
-    if not args.no_fp64 and prec == fluidgb.FL_CG_F32:
+    # The extended-precision CG forms on the same scene and schedule:
+    # float-float (FL_CG_F64) and IEEE double (FL_CG_F64_IEEE) reductions.
+    def precision_leg(form, what):
         q = p.copy()
-        q.cg_precision = fluidgb.FL_CG_F64
+        q.cg_precision = form
         g64 = fluidgb.Fluid(q, n)
         g64.set_stream(stream.cuda_stream)
         g64.set_particles(parts)
@@ -413,9 +413,16 @@ def run_ours(args):
         g64.sync()
         ms64 = timed_steps(torch, g64, args.steps)
         s64 = g64.stats()
-        fp64 = {"value": args.steps / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
-                "overhead_pct": 100.0 * (ms64 - ms) / ms, "last_cg_iterations": s64["cg_iterations"]}
         g64.close()
+        return {"value": args.steps / (ms64 / 1000.0), "ms_per_step": ms64 / args.steps,
+                "overhead_pct": 100.0 * (ms64 - ms) / ms, "last_cg_iterations": s64["cg_iterations"],
+                "reductions": what}
+
+    fp64 = fp64_ieee = None
+    if not args.no_fp64 and prec == fluidgb.FL_CG_F32:
+        fp64 = precision_leg(fluidgb.FL_CG_F64, "float-float (about 48-bit significand) on the FP32 pipe")
+        fp64_ieee = precision_leg(fluidgb.FL_CG_F64_IEEE, "IEEE double: exact products, double sums, trees, "
+                                                          "combines, alpha/beta and stopping test")
 
     # Multigrid-preconditioned CG (opt-in solver) on the same scene and schedule.
     mg = None
@@ -542,6 +549,7 @@ def run_ours(args):
             "stage_ms_per_step": {k: v / max(nprof, 1) for k, v in stage_ms.items()},
             "stage_roofline": stage_roofline,
             "fp64_reductions": fp64,
+            "fp64_ieee_reductions": fp64_ieee,
             "mgpcg": mg,
             "fwd_adjoint": adj,
             "configurations": legs or None,

@@ -85,6 +85,7 @@ struct CgShared {
     uint32_t layout, nslot;              // exchange slot layout (0 plan order, 1 lines, 2 one line per block), slots used
     float thr_f;                         // f32 stopping threshold on r.r
     float thr_dh, thr_dl;                // FL_CG_F64 stopping threshold on r.r (float-float)
+    double rs_d, thr_d;                  // FL_CG_F64_IEEE: r.r of the last exchange, stopping threshold
     float rs_hi, rs_lo;                  // r.r of the last exchange (rs_old); FL_CG_F32 uses rs_hi
     // Block-uniform loop bounds, read from shared memory where used (the cell
     // loops sit at the 64-register limit of a 1024-thread block).
@@ -95,6 +96,8 @@ struct CgShared {
 };
 static_assert(sizeof(CgShared) <= 227 * 1024, "CG shared memory exceeds the 227 KB per-block limit");
 static_assert(offsetof(CgShared, vals) % 16 == 0 && (VALS_HALF * 4) % 16 == 0, "resident operands are float4");
+static_assert(offsetof(CgShared, tree) % 8 == 0 && sizeof(CgShared::tree) >= 8 * CG_THREADS,
+              "the IEEE-double form stages its thread partials in the tree buffer");
 static_assert(VALS_HALF + 4 * 2 * CG_THREADS <= VAL_CAP + VAL_CAP / 32, "resident operands fit the upper half");
 
 // ---------------------------------------------------------------------------
@@ -218,6 +221,36 @@ __device__ __forceinline__ float chunk_tree(const float* s, uint32_t lane) {
     for (int o = 16; o > 0; o >>= 1) v = __fadd_rn(v, __shfl_down_sync(0xffffffffu, v, o));
     return v;
 }
+
+// Per-thread inner-product accumulator of the extended-precision forms:
+// float-float (FL_CG_F64: exact products by two-product, sums by two-sum on
+// the FP32 pipe) or IEEE double (FL_CG_F64_IEEE: f32 x f32 products are
+// exact in double; sums, trees and combines in double).
+template <int PREC>
+struct AccT {
+    using type = Df;
+};
+template <>
+struct AccT<FL_CG_F64_IEEE> {
+    using type = double;
+};
+__device__ __forceinline__ void acc_add(Df& a, float x, float y) { a = df_add(a, df_prod(x, y)); }
+// f32 x f32 is exact in double, so one fma = the exact product added with one rounding
+__device__ __forceinline__ void acc_add(double& a, float x, float y) { a = __fma_rn((double)x, (double)y, a); }
+__device__ __forceinline__ double warp_sum_d(double v) {  // result in lane 0
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_allsum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// a double's bits in two f32 slots (shared-memory staging and tagged words)
+__device__ __forceinline__ float d_lo(double v) { return __int_as_float(__double2loint(v)); }
+__device__ __forceinline__ float d_hi(double v) { return __int_as_float(__double2hiint(v)); }
+__device__ __forceinline__ double d_of(float lo, float hi) { return __hiloint2double(__float_as_int(hi), __float_as_int(lo)); }
 
 // FL_CG_F64: inner products accumulated in float-float (fl_device.cuh) by each
 // thread, across its block and across blocks; alpha and beta are float-float
@@ -357,7 +390,7 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
 // ---------------------------------------------------------------------------
 // The solve
 
-template <bool F64>
+template <int PREC>
 __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     CgShared& sh = *reinterpret_cast<CgShared*>(smem_raw);
@@ -365,12 +398,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     const DevParams& P = *b.prm;
     const uint32_t C = P.C, iters = P.iters < TAG_SPAN_MAX ? P.iters : TAG_SPAN_MAX, nchunks = P.nchunks;
     const uint32_t nx = P.nx, nxy = P.nx * P.ny;  // grids hold at most 2^30 cells
-    constexpr bool f64 = F64;
+    constexpr bool f64 = PREC != FL_CG_F32;       // no chunk trees: per-thread accumulators
+    constexpr bool ieee = PREC == FL_CG_F64_IEEE;
+    using Acc = typename AccT<PREC>::type;
     const float tol_sq = P.tol_sq;
     const double tol_sq_d = P.tol_sq_d;
     // Stopping test enabled: evaluated once (a double compare in the loop
     // would run on the FP64 pipe in every warp of every iteration).
-    const bool stop_on = F64 ? P.tol_sq_d > 0.0 : P.tol_sq > 0.0f;
+    const bool stop_on = f64 ? P.tol_sq_d > 0.0 : P.tol_sq > 0.0f;
     DevStats* st = b.st;
     const uint32_t G = gridDim.x, tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
     float* __restrict__ r = b.r;
@@ -624,14 +659,31 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // at 16*b), summed by warp 0 in a fixed order (lanes stride over blocks,
     // then a shuffle tree); lane 0 evaluates the post scalars (alpha, or beta
     // and the stopping test, from rs_old) and broadcasts them with the sum.
-    auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, int post, Df& out, float& sc,
+    auto reduce_df = [&](const unsigned long long* words, uint32_t tag, bool acq, int post, float& sc,
                          bool& dn) -> bool {
         const bool ok = stage_words(
             2 * G, tag, acq, st, b.prm, sh.vals,
             [&](uint32_t v) -> const unsigned long long* { return words + (v >> 1) * 16u + (v & 1u); },
             [&](uint32_t v) -> uint32_t { return v; });
         if (__syncthreads_or(!ok)) return false;
-        if (warp == 0) {
+        if (ieee && warp == 0) {  // the blocks' doubles, in the same fixed order
+            double v = 0.0;
+            for (uint32_t bb = lane; bb < G; bb += 32) v += d_of(sh.vals[2 * bb], sh.vals[2 * bb + 1]);
+            v = warp_sum_d(v);
+            if (lane == 0) {
+                const double rs_old = sh.rs_d;
+                float scv = 0.0f;
+                bool d2 = false;
+                if (post == 1) scv = fabs(v) > 1e-30 ? (float)(rs_old / v) : 0.0f;
+                if (post == 2) {
+                    scv = rs_old > 1e-30 ? (float)(v / rs_old) : 0.0f;
+                    d2 = stop_on && v <= sh.thr_d;
+                    sh.rs_d = v;
+                }
+                sh.scal[2] = scv;
+                sh.scal[3] = d2 ? 1.0f : 0.0f;
+            }
+        } else if (warp == 0) {
             Df acc = {0.0f, 0.0f};
             for (uint32_t bb = lane; bb < G; bb += 32) acc = df_add(acc, Df{sh.vals[2 * bb], sh.vals[2 * bb + 1]});
             acc = warp_sum_df(acc);
@@ -653,27 +705,47 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             }
         }
         __syncthreads();
-        out = Df{sh.scal[0], sh.scal[1]};
         sc = sh.scal[2];
         dn = sh.scal[3] != 0.0f;
         return true;
     };
-    // Block float-float partial published as two tagged words on the block's line.
-    auto publish_df = [&](Df acc, unsigned long long* words, uint32_t tag, bool rel) {
-        acc = warp_sum_df(acc);
-        if (lane == 0) {
-            sh.red[2 * warp] = acc.hi;
-            sh.red[2 * warp + 1] = acc.lo;
-        }
-        __syncthreads();
-        if (warp == 0) {
-            Df v = {sh.red[2 * lane], sh.red[2 * lane + 1]};
-            v = warp_sum_df(v);
-            // lanes 0 and 1 store {hi, lo} in one instruction (the FP64-reduction
-            // CG stage measured 1.96-1.98 vs 2.10-2.13 ms per substep at 128^3
-            // against two stores by lane 0: readers saw hi before lo)
-            const float lo = __shfl_sync(0xffffffffu, v.lo, 0);
-            if (lane < 2) publish(words + 16 * blockIdx.x + lane, tag, lane ? lo : v.hi, rel);
+    // Block partial published as two tagged words on the block's line: the
+    // float-float {hi, lo}, or a double's low and high 32 bits.
+    auto publish_df = [&](Acc acc, unsigned long long* words, uint32_t tag, bool rel) {
+        if constexpr (ieee) {
+            // The FP64 pipe (about 2 lane-operations per clock per SM) is the
+            // bound: warp 0 sums the 1024 thread partials (lane l: partials l,
+            // l + 32, ... in sequence, then a 5-level tree) instead of a tree
+            // in every warp (36 double adds per block instead of 160).  The
+            // partials are staged in the chunk-tree buffer, which the
+            // extended-precision forms do not use (the exchange window is
+            // written by the other warps' polls while warp 0 reads).
+            double* part = reinterpret_cast<double*>(&sh.tree[0][0]);
+            part[tid] = acc;
+            __syncthreads();
+            if (warp == 0) {
+                double s = 0.0;
+                for (uint32_t t2 = lane; t2 < (uint32_t)CG_THREADS; t2 += 32) s += part[t2];
+                const double v = warp_sum_d(s);
+                const float lo = __shfl_sync(0xffffffffu, d_lo(v), 0), hi = __shfl_sync(0xffffffffu, d_hi(v), 0);
+                if (lane < 2) publish(words + 16 * blockIdx.x + lane, tag, lane ? hi : lo, rel);
+            }
+        } else {
+            acc = warp_sum_df(acc);
+            if (lane == 0) {
+                sh.red[2 * warp] = acc.hi;
+                sh.red[2 * warp + 1] = acc.lo;
+            }
+            __syncthreads();
+            if (warp == 0) {
+                Df v = {sh.red[2 * lane], sh.red[2 * lane + 1]};
+                v = warp_sum_df(v);
+                // lanes 0 and 1 store {hi, lo} in one instruction (the FP64-reduction
+                // CG stage measured 1.96-1.98 vs 2.10-2.13 ms per substep at 128^3
+                // against two stores by lane 0: readers saw hi before lo)
+                const float lo = __shfl_sync(0xffffffffu, v.lo, 0);
+                if (lane < 2) publish(words + 16 * blockIdx.x + lane, tag, lane ? lo : v.hi, rel);
+            }
         }
     };
     // Warp w evaluates the trees of chunks j0 + w and j0 + w + 32 of the pass
@@ -708,7 +780,26 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // Initial residual norm (cg_init.wgsl + cg_reduce of r.r).
     float rs_init_f = 0.0f;
     Df rs_init_d = {0.0f, 0.0f};
-    if (f64) {
+    if (ieee) {  // the chunks' float-float partials (exact in double), summed in double
+        double acc = 0.0;
+        for (uint32_t e = tid; e < A; e += CG_THREADS) {
+            const float2 v = b.chunk_rr_df[plan[e]];
+            acc += (double)v.x + (double)v.y;
+        }
+        acc = warp_allsum_d(acc);
+        if (lane == 0) {
+            sh.red[2 * warp] = d_lo(acc);
+            sh.red[2 * warp + 1] = d_hi(acc);
+        }
+        __syncthreads();
+        const double rs0 = warp_allsum_d(d_of(sh.red[2 * lane], sh.red[2 * lane + 1]));
+        if (tid == 0) {
+            sh.rs_d = rs0;
+            sh.thr_d = P.thr_abs ? P.thr_abs_d : tol_sq_d * rs0;
+            if (blockIdx.x == 0) st->rs_init = rs0;
+        }
+        __syncthreads();  // sh.red is reused
+    } else if (f64) {
         Df acc = {0.0f, 0.0f};
         for (uint32_t e = tid; e < A; e += CG_THREADS) {
             const float2 v = b.chunk_rr_df[plan[e]];
@@ -740,7 +831,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // absolute threshold.
     if (tid == 0) {
         if (!f64) sh.thr_f = P.thr_abs ? P.thr_abs_f : __fmul_rn(tol_sq, rs_init_f);
-        if (blockIdx.x == 0) st->rs_init = f64 ? df_to_double(rs_init_d) : (double)rs_init_f;
+        if (blockIdx.x == 0 && !ieee) st->rs_init = f64 ? df_to_double(rs_init_d) : (double)rs_init_f;
     }
     __syncthreads();
 
@@ -752,7 +843,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         const bool first = it == 0;
         const float* __restrict__ d_src = first ? d_cur : d_prev;
         // ---------------- phase 1: direction + SpMV + d.q ----------------
-        Df acc = {0.0f, 0.0f};
+        Acc acc{};
         tag++;
         if (vld(sh.u_res)) {  // resident operands: own d, r from shared memory, neighbours' from global
             uint32_t ent[2], cc[2];
@@ -793,7 +884,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 if (!first) d_cur[cc[u]] = dc;
                 rv4[tu].x = dc;
                 rv4[tu].z = qc;
-                if (f64) acc = df_add(acc, df_prod(dc, qc));
+                if (f64) acc_add(acc, dc, qc);
                 else sh.tree[info >> 18][(info >> 10) & 255u] = __fmul_rn(dc, qc);
             }
             if (!f64) publish_trees(0, vld(sh.u_mc), slotA, tag, false);
@@ -845,7 +936,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         const uint32_t c = cc[u];
                         if (!first) d_cur[c] = dc;
                         q[c] = qc;
-                        if (f64) acc = df_add(acc, df_prod(dc, qc));
+                        if (f64) acc_add(acc, dc, qc);
                         else sh.tree[(info >> 18) - j0][(info >> 10) & 255u] = __fmul_rn(dc, qc);
                     }
                 }
@@ -877,7 +968,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         const float qc = __fsub_rn(__fmul_rn((float)((info >> 7) & 7u), dc), sum);
                         if (!first) d_cur[c] = dc;
                         q[c] = qc;
-                        if (f64) acc = df_add(acc, df_prod(dc, qc));
+                        if (f64) acc_add(acc, dc, qc);
                         prod = __fmul_rn(dc, qc);
                     }
                     if (!f64) sh.tree[t / CHUNK][cl] = prod;
@@ -893,15 +984,14 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             bool dn_unused;
             if (f64) {
                 publish_df(acc, wordA, tag, false);
-                Df dq;
-                if (!reduce_df(wordA, tag, false, 1, dq, alpha, dn_unused)) return;
+                if (!reduce_df(wordA, tag, false, 1, alpha, dn_unused)) return;
             } else {
                 float dq;
                 if (!reduce_f32(slotA, segA, tag, false, 1, dq, alpha, dn_unused)) return;
             }
         }
         // ---------------- phase 2: update + r.r ----------------
-        acc = {0.0f, 0.0f};
+        acc = Acc{};
         tag++;
         if (vld(sh.u_res)) {  // every operand in shared memory; r also to global for the neighbours
 #pragma unroll
@@ -915,7 +1005,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 r[sh.chunk[e >> 18] * CHUNK + ((e >> 10) & 255u)] = rc;
                 rv4[tu].y = rc;
                 rv4[tu].w = pn;
-                if (f64) acc = df_add(acc, df_prod(rc, rc));
+                if (f64) acc_add(acc, rc, rc);
                 else sh.tree[e >> 18][(e >> 10) & 255u] = __fmul_rn(rc, rc);
             }
             if (!f64) publish_trees(0, vld(sh.u_mc), slotB, tag, true);
@@ -949,7 +1039,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         p[c] = __fadd_rn(pv[u], __fmul_rn(alpha, dv[u]));       // cg_update.wgsl:33
                         const float rc = __fsub_rn(rv[u], __fmul_rn(alpha, qv[u]));  // cg_update.wgsl:34
                         r[c] = rc;
-                        if (f64) acc = df_add(acc, df_prod(rc, rc));
+                        if (f64) acc_add(acc, rc, rc);
                         else sh.tree[(ent[u] >> 18) - j0][(ent[u] >> 10) & 255u] = __fmul_rn(rc, rc);
                     }
                 }
@@ -970,7 +1060,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         p[c] = __fadd_rn(p[c], __fmul_rn(alpha, d_cur[c]));
                         const float rc = __fsub_rn(r[c], __fmul_rn(alpha, q[c]));
                         r[c] = rc;
-                        if (f64) acc = df_add(acc, df_prod(rc, rc));
+                        if (f64) acc_add(acc, rc, rc);
                         prod = __fmul_rn(rc, rc);
                     }
                     if (!f64) sh.tree[t / CHUNK][cl] = prod;
@@ -985,8 +1075,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         bool done;
         if (f64) {
             publish_df(acc, wordB, tag, true);
-            Df rs_new;
-            if (!reduce_df(wordB, tag, true, 2, rs_new, beta, done)) return;
+            if (!reduce_df(wordB, tag, true, 2, beta, done)) return;
         } else {
             float rs_new;
             if (!reduce_f32(slotB, segB, tag, true, 2, rs_new, beta, done)) return;
@@ -1000,19 +1089,22 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         }
     if (blockIdx.x == 0 && tid == 0) {
         st->cg_iters = k;
-        st->rs_final = f64 ? df_to_double(Df{sh.rs_hi, sh.rs_lo}) : (double)sh.rs_hi;
+        st->rs_final = ieee ? sh.rs_d : (f64 ? df_to_double(Df{sh.rs_hi, sh.rs_lo}) : (double)sh.rs_hi);
     }
 }
 
 int cg_max_blocks_per_sm() {
-    int n[2] = {0, 0};
-    for (int i = 0; i < 2; i++) {
-        const void* f = i ? (const void*)k_cg<true> : (const void*)k_cg<false>;
-        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CgShared)) != cudaSuccess)
+    const void* fs[3] = {(const void*)k_cg<FL_CG_F32>, (const void*)k_cg<FL_CG_F64>, (const void*)k_cg<FL_CG_F64_IEEE>};
+    int lo = 1 << 30;
+    for (int i = 0; i < 3; i++) {
+        int n = 0;
+        if (cudaFuncSetAttribute(fs[i], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(CgShared)) !=
+            cudaSuccess)
             return 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n[i], f, CG_THREADS, sizeof(CgShared)) != cudaSuccess) return 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fs[i], CG_THREADS, sizeof(CgShared)) != cudaSuccess) return 0;
+        lo = n < lo ? n : lo;
     }
-    return n[0] < n[1] ? n[0] : n[1];
+    return lo;
 }
 
 cudaError_t launch_cg_plan(const DevBufs& b, uint32_t G, cudaStream_t s) {
@@ -1021,7 +1113,8 @@ cudaError_t launch_cg_plan(const DevBufs& b, uint32_t G, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, bool f64) {
+cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, uint32_t precision) {
+    if (precision > FL_CG_F64_IEEE) return cudaErrorInvalidValue;
     if (L.cg_blocks < 1 || (uint32_t)L.cg_blocks > MAX_CG_BLOCKS) return cudaErrorInvalidValue;
     k_cg_plan<<<1, CHUNK, 0, s>>>(b, (uint32_t)L.cg_blocks);
     cudaError_t e = cudaGetLastError();
@@ -1036,7 +1129,8 @@ cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, bool
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    return f64 ? cudaLaunchKernelEx(&cfg, k_cg<true>, b) : cudaLaunchKernelEx(&cfg, k_cg<false>, b);
+    if (precision == FL_CG_F64_IEEE) return cudaLaunchKernelEx(&cfg, k_cg<FL_CG_F64_IEEE>, b);
+    return precision == FL_CG_F64 ? cudaLaunchKernelEx(&cfg, k_cg<FL_CG_F64>, b) : cudaLaunchKernelEx(&cfg, k_cg<FL_CG_F32>, b);
 }
 
 }  // namespace fl

@@ -285,8 +285,8 @@ cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s);
 cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz,
                        cudaStream_t s);
 cudaError_t launch_grid_prep(const DevBufs& b, uint32_t C, cudaStream_t s);
-// f64: FL_CG_F64 (the kernel is specialised per precision).
-cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, bool f64);
+// precision: FL_CG_F32, FL_CG_F64 or FL_CG_F64_IEEE (the kernel is specialised per precision).
+cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, uint32_t precision);
 cudaError_t launch_project(const DevBufs& b, uint32_t C, cudaStream_t s);
 cudaError_t launch_g2p(const DevBufs& b, const LaunchCfg& L, cudaStream_t s);
 cudaError_t launch_iota(uint32_t* ids, uint32_t n, cudaStream_t s);

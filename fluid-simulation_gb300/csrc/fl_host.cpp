@@ -101,7 +101,10 @@ fl_status validate(const fl_params* p, std::string* why) {
     if (!(p->geom[0] > 0.0f) || !(p->geom[1] > 0.0f)) { *why = "h and inv_h must be > 0"; return FL_INVALID_ARG; }
     if (!(p->geom[2] > 0.0f)) { *why = "dt must be > 0"; return FL_INVALID_ARG; }
     if (!(p->phys[1] > 0.0f)) { *why = "rho must be > 0"; return FL_INVALID_ARG; }
-    if (p->cg_precision > 1u) { *why = "cg_precision must be FL_CG_F32 or FL_CG_F64"; return FL_INVALID_ARG; }
+    if (p->cg_precision > FL_CG_F64_IEEE) {
+        *why = "cg_precision must be FL_CG_F32, FL_CG_F64 or FL_CG_F64_IEEE";
+        return FL_INVALID_ARG;
+    }
     if (p->advect_order > 2u) { *why = "advect_order must be 1 or 2"; return FL_INVALID_ARG; }
     if (p->pressure_solver > 1u) { *why = "pressure_solver must be FL_SOLVER_CG or FL_SOLVER_MGPCG"; return FL_INVALID_ARG; }
     for (int i = 0; i < 3; i++)
@@ -269,7 +272,7 @@ cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEve
             return e;
     } else if (h->prm.pressure_solver == FL_SOLVER_MGPCG) {
         if ((e = fl::launch_mgpcg(b, h->mg, h->L, s)) != cudaSuccess) return e;
-    } else if ((e = fl::launch_cg(b, h->L, s, h->prm.cg_precision == FL_CG_F64)) != cudaSuccess) {
+    } else if ((e = fl::launch_cg(b, h->L, s, h->prm.cg_precision)) != cudaSuccess) {
         return e;
     }
     if ((e = mark(5)) != cudaSuccess) return e;
@@ -869,7 +872,7 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
     if (nx < 3 || ny < 3 || nz < 3 || (uint64_t)nx * ny * nz > (1ull << 30))
         return set_err(nullptr, FL_INVALID_ARG, "bad grid size");
     if (!(h > 0.0f) || !(rho > 0.0f) || !(dt > 0.0f)) return set_err(nullptr, FL_INVALID_ARG, "h, rho, dt must be > 0");
-    if (cg_precision > 1u) return set_err(nullptr, FL_INVALID_ARG, "bad cg_precision");
+    if (cg_precision > FL_CG_F64_IEEE) return set_err(nullptr, FL_INVALID_ARG, "bad cg_precision");
     fl_status s = device_check(nullptr);
     if (s != FL_OK) return s;
     fl_params prm;
@@ -930,7 +933,7 @@ fl_status fl_solve_pressure(uint32_t nx, uint32_t ny, uint32_t nz, const uint8_t
         if ((e = cudaMemcpyAsync(ddiv, divergence, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
         if (warm_start && (e = cudaMemcpyAsync(b.p, pressure_in, 4 * C, cudaMemcpyHostToDevice, st)) != cudaSuccess) break;
         if ((e = fl::launch_solve_init(b, (uint32_t)C, ddiv, st)) != cudaSuccess) break;
-        if ((e = fl::launch_cg(b, L, st, cg_precision == FL_CG_F64)) != cudaSuccess) break;
+        if ((e = fl::launch_cg(b, L, st, cg_precision)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(pressure_out, b.p, 4 * C, cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
         if ((e = cudaMemcpyAsync(&ds, b.st, sizeof(ds), cudaMemcpyDeviceToHost, st)) != cudaSuccess) break;
         e = cudaStreamSynchronize(st);
@@ -1362,7 +1365,7 @@ fl_status fl_step_adjoint(fl_handle* h, fl_tape* t, const void* dL_dout_dev, voi
         if (ms != FL_OK) return ms;
         FL_CUDA(h, fl::launch_mgpcg(cg, t->mg, h->L, st));
     } else {
-        FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision == FL_CG_F64));
+        FL_CUDA(h, fl::launch_cg(cg, h->L, st, h->prm.cg_precision));
     }
     FL_CUDA(h, fl::launch_adj_faces(a, h->F3, st));
     FL_CUDA(h, fl::launch_adj_p2g(a, h->L, st));

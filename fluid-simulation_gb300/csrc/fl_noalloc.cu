@@ -192,7 +192,7 @@ extern "C" fl_status fl_solve_pressure_noalloc(uint32_t nx, uint32_t ny, uint32_
     if ((e = cudaGetLastError()) != cudaSuccess) return fail(FL_CUDA_ERROR, std::string("setup: ") + cudaGetErrorString(e));
     if ((e = fl::launch_solve_init(b, d.C, divergence_dev, st)) != cudaSuccess)
         return fail(FL_CUDA_ERROR, std::string("init: ") + cudaGetErrorString(e));
-    if ((e = fl::launch_cg(b, L, st, cg_precision == FL_CG_F64)) != cudaSuccess)
+    if ((e = fl::launch_cg(b, L, st, cg_precision)) != cudaSuccess)
         return fail(FL_CUDA_ERROR, std::string("cg: ") + cudaGetErrorString(e));
     fl::DevStats ds;
     if ((e = cudaMemcpyAsync(&ds, b.st, sizeof(ds), cudaMemcpyDeviceToHost, st)) != cudaSuccess)

@@ -16,7 +16,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libfluidgb.so")
 
 FL_OK, FL_INVALID_ARG, FL_OOM, FL_CUDA_ERROR, FL_NOT_CONVERGED, FL_TIMEOUT, FL_NO_DEVICE, FL_INTERNAL = range(8)
 FL_CELL_SOLID, FL_CELL_LIQUID, FL_CELL_AIR = 0, 1, 2
-FL_CG_F32, FL_CG_F64 = 0, 1
+FL_CG_F32, FL_CG_F64, FL_CG_F64_IEEE = 0, 1, 2
 FL_SOLVER_CG, FL_SOLVER_MGPCG = 0, 1
 FL_SOLVER_FOLLOW = 0xFFFFFFFF
 FL_RELAX_JACOBI, FL_RELAX_RBGS = 0, 1

@@ -48,12 +48,16 @@ typedef enum fl_status {
  * (app/crates/fluid-lab/src/sim/mod.rs:30-36). */
 enum { FL_CELL_SOLID = 0, FL_CELL_LIQUID = 1, FL_CELL_AIR = 2 };
 
-/* CG inner-product precision (extension field `cg_precision`). */
+/* CG inner-product precision (extension field `cg_precision`).  The FP32
+ * vector arithmetic (directions, SpMV, updates) is the same in all three. */
 enum {
-    FL_CG_F32 = 0, /* reference arithmetic: f32 two-level 256-wide tree dots (cg_reduce.wgsl) */
-    FL_CG_F64 = 1  /* extended-precision inner products, residual norm and convergence
-                      test (float-float, ~48-bit significand; the FP32 vector arithmetic
-                      is unchanged) */
+    FL_CG_F32 = 0,      /* reference arithmetic: f32 two-level 256-wide tree dots (cg_reduce.wgsl) */
+    FL_CG_F64 = 1,      /* extended-precision inner products, residual norm and convergence
+                           test in float-float (~48-bit significand) on the FP32 pipe */
+    FL_CG_F64_IEEE = 2  /* inner products, residual norm, alpha/beta quotients and convergence
+                           test in IEEE double: exact f32 x f32 products, double sums, trees and
+                           combines (the CPU reference CG's f64 dot, sim/pressure.rs:182-188);
+                           the initial residual's per-chunk partials are float-float */
 };
 
 /*
@@ -76,7 +80,7 @@ typedef struct fl_params {
     float pressure_tolerance; /* relative residual tolerance; 0 = off; clamped to
                                  [0, 0.1] like set_pressure_residual_tolerance
                                  (fluid.rs:47-50, :1362-1369) */
-    uint32_t cg_precision;    /* FL_CG_F32 or FL_CG_F64 */
+    uint32_t cg_precision;    /* FL_CG_F32, FL_CG_F64 or FL_CG_F64_IEEE */
     uint32_t advect_order;    /* 1 = forward Euler (reference g2p.wgsl:186); 2 = midpoint */
     uint32_t sort_period;     /* accepted for drop-in compatibility; the layout is
                                  re-sorted every substep (the gather-form P2G reads bins) */

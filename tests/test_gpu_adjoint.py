@@ -14,7 +14,7 @@ position derivative, put the 4-step gradient off by 66%.
 import numpy as np
 import pytest
 
-from fluidgb import FL_CG_F64, scenes
+from fluidgb import FL_CG_F64, FL_CG_F64_IEEE, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -341,3 +341,17 @@ def test_backward_passes_repeat_bit_for_bit(case):
     roll.close()
     assert np.all(np.isfinite(a[0])) and np.any(a[0] != 0)
     assert np.array_equal(g1.cpu().numpy(), a[0]) and np.array_equal(np.asarray(gg1), a[1])
+
+
+def test_adjoint_with_ieee_double_reductions(oracle):
+    """The adjoint pressure solve follows the handle's cg_precision: with
+    IEEE-double inner products the 4-substep gradients meet the same 1e-3
+    bound against the FP64 oracle's finite differences."""
+    pytest.importorskip("torch")
+    p, parts, steps = setup_case(steps=4)
+    p.cg_precision = FL_CG_F64_IEEE
+    gv, gg = adjoint_grads(p, parts, steps, 2)
+    errs = fd_errors(oracle, p, parts, steps, gv, gg)
+    print("IEEE-double CG, 4 steps: rel errors %s" % (["%.2e" % e for e in errs]))
+    assert len(errs) >= 2
+    assert max(errs) < 1e-3, errs

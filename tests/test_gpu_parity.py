@@ -9,7 +9,7 @@ a stated tolerance.
 import numpy as np
 import pytest
 
-from fluidgb import FL_CG_F64, Fluid, scenes
+from fluidgb import FL_CG_F64, FL_CG_F64_IEEE, Fluid, scenes
 from fluidgb import _abi
 
 pytestmark = pytest.mark.gpu
@@ -179,11 +179,13 @@ def test_empty_and_tiny_particle_sets(lib, oracle):
         assert_same_state(g, o, "n=%d" % n)
 
 
-def test_fp64_reductions_match_oracle_to_tolerance(lib, oracle):
-    """FL_CG_F64: inner products in double.  Summation order differs from the
+@pytest.mark.parametrize("form", [FL_CG_F64, FL_CG_F64_IEEE], ids=["float-float", "ieee-double"])
+def test_fp64_reductions_match_oracle_to_tolerance(lib, oracle, form):
+    """FL_CG_F64 (float-float) and FL_CG_F64_IEEE (double) inner products
+    against the oracle's double dots.  Summation order differs from the
     oracle's (1e-16 relative), so alpha/beta may differ in the last f32 bit;
     state must agree to 1e-5 relative after 3 steps."""
-    p, parts, _ = scenes.workload("dam32", precision=FL_CG_F64)
+    p, parts, _ = scenes.workload("dam32", precision=form)
     g, o = make_pair(oracle, p, parts)
     g.step(3)
     o.step(3)
@@ -200,7 +202,7 @@ def test_fp64_reductions_match_oracle_to_tolerance(lib, oracle):
     assert abs(g.stats()["cg_iterations"] - o.stats()["cg_iterations"]) <= 1
 
 
-@pytest.mark.parametrize("precision", [0, FL_CG_F64])
+@pytest.mark.parametrize("precision", [0, FL_CG_F64, FL_CG_F64_IEEE])
 def test_gpu_run_is_deterministic(lib, precision):
     p, parts, _ = scenes.workload("dam32", precision=precision)
     outs = []
@@ -286,9 +288,10 @@ def test_solve_pressure_matches_oracle_and_reference_thresholds(lib, oracle):
                                      tolerance=0.1)
     assert np.array_equal(pw, pwo) and sw["cg_iterations"] == swo["cg_iterations"] < 40
     # f64 inner products
-    p64, s64 = _abi.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, precision=FL_CG_F64)
     o64, _ = oracle.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, precision=1)
-    assert np.allclose(p64, o64, rtol=1e-5, atol=1e-5 * np.abs(o64).max())
+    for form in (FL_CG_F64, FL_CG_F64_IEEE):
+        p64, s64 = _abi.solve_pressure(ct, div0, d, 1.0, 1.0, 1.0, 40, precision=form)
+        assert np.allclose(p64, o64, rtol=1e-5, atol=1e-5 * np.abs(o64).max()), form
 
 
 def test_128_grid_one_step_bit_exact(lib, oracle):
@@ -346,14 +349,15 @@ def test_128_grid_thirty_steps_bit_exact(lib, oracle):
     o.close()
 
 
-def test_128_grid_fp64_reductions_track_the_oracle(lib, oracle):
-    """FL_CG_F64 on the benchmarked configuration, 20 substeps.  Before every
-    substep the oracle (the reference step with double inner products) takes
-    the GPU's particles and warm-start pressure, and both take the step; the
-    float-float reductions then agree with the double ones to 1e-5 relative in
-    face velocity and pressure, 1e-6 in position, and in the iteration count
-    to within one."""
-    p, parts, _ = scenes.workload("dam128_2m", precision=FL_CG_F64)
+@pytest.mark.parametrize("form", [FL_CG_F64, FL_CG_F64_IEEE], ids=["float-float", "ieee-double"])
+def test_128_grid_fp64_reductions_track_the_oracle(lib, oracle, form):
+    """The extended-precision forms on the benchmarked configuration, 20
+    substeps.  Before every substep the oracle (the reference step with double
+    inner products) takes the GPU's particles and warm-start pressure, and
+    both take the step; the float-float or IEEE-double reductions then agree
+    with the oracle's to 1e-5 relative in face velocity and pressure, 1e-6 in
+    position, and in the iteration count to within one."""
+    p, parts, _ = scenes.workload("dam128_2m", precision=form)
     n = parts.shape[0]
     g = Fluid(p, n)
     g.set_particles(parts)
@@ -381,7 +385,7 @@ def test_128_grid_fp64_reductions_track_the_oracle(lib, oracle):
         assert dv <= 1e-5 and dp <= 1e-5 and dx <= 1e-6, (s, dv, dp, dx)
         assert abs(g.stats()["cg_iterations"] - o.stats()["cg_iterations"]) <= 1, s
         assert g.stats()["device_status"] == 0
-    print("FL_CG_F64 vs oracle over 20 substeps of dam128_2m: max rel velocity %.2e, pressure %.2e, "
-          "max abs position %.2e" % (worst["velocity"], worst["pressure"], worst["position"]))
+    print("form %d vs oracle over 20 substeps of dam128_2m: max rel velocity %.2e, pressure %.2e, "
+          "max abs position %.2e" % (form, worst["velocity"], worst["pressure"], worst["position"]))
     g.close()
     o.close()

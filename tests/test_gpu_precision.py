@@ -4,7 +4,8 @@ Scene: a sphere of radius 0.12 at (0.5, 0.75, 0.5) falling into a pool of
 depth 0.3, 8 jittered particles per fluid cell, seed 0x5EED, 200 substeps.  For
 each CG relative tolerance in {1e-3, 1e-4, 1e-5, 1e-6} and each form (the
 reference's FP32 CG, FL_CG_F32, and the form with extended-precision
-reductions, FL_CG_F64), the GPU runs the scene; at substeps 1 and 200 the step
+reductions in float-float, FL_CG_F64, and in IEEE double, FL_CG_F64_IEEE),
+the GPU runs the scene; at substeps 1 and 200 the step
 is repeated by the FP64 oracle from the GPU's state before it (particles and
 the warm-start pressure), once at the same tolerance and iteration cap and once
 converged (tolerance 1e-10).  Reported per step, max and RMS of
@@ -30,7 +31,7 @@ import os
 import numpy as np
 import pytest
 
-from fluidgb import FL_CG_F32, FL_CG_F64, Fluid, scenes
+from fluidgb import FL_CG_F32, FL_CG_F64, FL_CG_F64_IEEE, Fluid, scenes
 
 pytestmark = pytest.mark.gpu
 
@@ -77,7 +78,7 @@ def test_precision_study_sphere_pool128(lib_built, oracle):
     results = []
     try:
         for tol in TOLS:
-            for prec in (FL_CG_F32, FL_CG_F64):
+            for prec in (FL_CG_F32, FL_CG_F64, FL_CG_F64_IEEE):
                 p = params(prec, tol, spec["iters"])
                 g = Fluid(p, n)
                 g.set_particles(parts)
@@ -95,7 +96,8 @@ def test_precision_study_sphere_pool128(lib_built, oracle):
                     assert st["device_status"] == 0
                     by_id = np.empty_like(x1)
                     by_id[id1] = x1
-                    row = {"tol": tol, "form": "f32" if prec == FL_CG_F32 else "f64-reductions", "step": k,
+                    row = {"tol": tol, "form": {FL_CG_F32: "f32", FL_CG_F64: "f64-reductions",
+                                                    FL_CG_F64_IEEE: "ieee-f64-reductions"}[prec], "step": k,
                            "cg_iterations": st["cg_iterations"], "particles": n}
                     for label, otol, oiters in (("same_tol", tol, spec["iters"]), ("converged", 1e-10, 5000)):
                         q = params(FL_CG_F32, otol, oiters)

@@ -568,16 +568,16 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                     }
                     __syncwarp();
                     if (lane == 0) {  // cg_reduce_final.wgsl:29-36: in plan order, from +0
+                        // entries past the segment's end were staged as +0,
+                        // which leaves s (never -0) unchanged
                         const uint32_t n = hi - e0 < 128u ? hi - e0 : 128u;
-                        uint32_t j = 0;
-                        for (; j + 8 <= n; j += 8) {
-                            float t8[8];
+                        for (uint32_t j = 0; j < n; j += 16) {
+                            float t16[16];
 #pragma unroll
-                            for (int k2 = 0; k2 < 8; k2++) t8[k2] = buf[j + k2];
+                            for (int k2 = 0; k2 < 16; k2++) t16[k2] = buf[j + k2];
 #pragma unroll
-                            for (int k2 = 0; k2 < 8; k2++) s = __fadd_rn(s, t8[k2]);
+                            for (int k2 = 0; k2 < 16; k2++) s = __fadd_rn(s, t16[k2]);
                         }
-                        for (; j < n; j++) s = __fadd_rn(s, buf[j]);
                     }
                     __syncwarp();
                 }
@@ -628,17 +628,20 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             }
             if (__syncthreads_or(!ok)) return false;
             if (tid < (uint32_t)CHUNK) {
+                // 16 loads first (past the segment's end: +0), then the
+                // sequential adds.  acc starts at +0 and a sum of floats is
+                // -0 only when both terms are, so acc is never -0 and adding
+                // +0 leaves it unchanged: the fold equals the loop over
+                // [lo, hi) exactly, with no per-lane tail loop.
                 const uint32_t lo = sh.off[tid] > w0 ? sh.off[tid] : w0;
                 const uint32_t hi = sh.off[tid + 1] < w0 + wn ? sh.off[tid + 1] : w0 + wn;
-                uint32_t e = lo;
-                for (; e + 8 <= hi; e += 8) {  // loads first, then the sequential adds
-                    float v[8];
+                for (uint32_t e = lo; e < hi; e += 16) {
+                    float v[16];
 #pragma unroll
-                    for (int k2 = 0; k2 < 8; k2++) v[k2] = sh.vals[vpos(e - w0 + k2)];
+                    for (int k2 = 0; k2 < 16; k2++) v[k2] = e + k2 < hi ? sh.vals[vpos(e - w0 + k2)] : 0.0f;
 #pragma unroll
-                    for (int k2 = 0; k2 < 8; k2++) acc = __fadd_rn(acc, v[k2]);
+                    for (int k2 = 0; k2 < 16; k2++) acc = __fadd_rn(acc, v[k2]);
                 }
-                for (; e < hi; e++) acc = __fadd_rn(acc, sh.vals[vpos(e - w0)]);
             }
             if (w0 + wn < A) __syncthreads();
         }

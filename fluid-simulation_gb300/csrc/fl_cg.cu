@@ -49,6 +49,7 @@ namespace fl {
 constexpr int CG_WARPS = CG_THREADS / 32;
 constexpr uint32_t KT = 2 * CG_WARPS;    // chunks per tree pass: two chunk trees per warp
 constexpr uint32_t CELL_CAP = 16384;     // liquid cells listed per block
+constexpr uint32_t QCAP = CELL_CAP / 2;  // quads listed per block (8 bytes each, in the same array)
 constexpr uint32_t KCH = 2048;           // chunk ids cached per block
 constexpr uint32_t VAL_CAP = 16384;      // chunk partials staged per window
 constexpr uint32_t MAX_PASS = KCH / KT;  // cached tree passes
@@ -89,13 +90,15 @@ struct CgShared {
     float rs_hi, rs_lo;                  // r.r of the last exchange (rs_old); FL_CG_F32 uses rs_hi
     // Block-uniform loop bounds, read from shared memory where used (the cell
     // loops sit at the 64-register limit of a 1024-thread block).
-    uint32_t u_s0, u_m, u_mc, u_npc, u_ncell, u_res;
+    uint32_t u_s0, u_m, u_mc, u_npc, u_ncell, u_res, u_quad, u_lb;
     uint32_t bstart[MAX_CG_BLOCKS + 1];  // first plan entry of every block
     uint32_t spos[MAX_CG_BLOCKS + 1];    // first exchange slot of every block
     uint16_t lineblk[VAL_CAP / 16 + MAX_CG_BLOCKS];  // line of the slot area -> owning block
 };
 static_assert(sizeof(CgShared) <= 227 * 1024, "CG shared memory exceeds the 227 KB per-block limit");
 static_assert(offsetof(CgShared, vals) % 16 == 0 && (VALS_HALF * 4) % 16 == 0, "resident operands are float4");
+static_assert(offsetof(CgShared, tree) % 16 == 0 && offsetof(CgShared, cell) % 8 == 0,
+              "quad layout: float4 tree slots, 8-byte quad entries");
 static_assert(offsetof(CgShared, tree) % 8 == 0 && sizeof(CgShared::tree) >= 8 * CG_THREADS,
               "the IEEE-double form stages its thread partials in the tree buffer");
 static_assert(VALS_HALF + 4 * 2 * CG_THREADS <= VAL_CAP + VAL_CAP / 32, "resident operands fit the upper half");
@@ -203,6 +206,17 @@ __device__ __forceinline__ bool stage_words(uint32_t nvirt, uint32_t tag, bool a
 // without the pad the segment sums ran 16-way bank conflicted (0.85 vs
 // 0.47 us per exchange at 128^3).
 __device__ __forceinline__ uint32_t vpos(uint32_t e) { return e + (e >> 5); }
+
+// float4 access to the CG vectors in the quad layout (16-byte aligned quads)
+__device__ __forceinline__ float4 ld_f4(const float* a) { return *reinterpret_cast<const float4*>(a); }
+__device__ __forceinline__ void st_f4(float* a, float4 v) { *reinterpret_cast<float4*>(a) = v; }
+__device__ __forceinline__ float f4_at(const float4& v, int k) { return k == 0 ? v.x : k == 1 ? v.y : k == 2 ? v.z : v.w; }
+__device__ __forceinline__ void f4_set(float4& v, int k, float x) {
+    if (k == 0) v.x = x;
+    else if (k == 1) v.y = x;
+    else if (k == 2) v.z = x;
+    else v.w = x;
+}
 
 // A block-uniform value read from shared memory at its use (not kept in a register).
 __device__ __forceinline__ uint32_t vld(const uint32_t& x) { return *(const volatile uint32_t*)&x; }
@@ -449,10 +463,69 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     __syncthreads();
     const uint32_t A = sh.off[CHUNK];
 
-    // List the liquid cells of chunks [0, mc), four chunks per round, in
-    // (chunk, cell) order; stop before CELL_CAP would be exceeded.
+    // Quad layout: when rows are a multiple of four cells and the vectors are
+    // 16-byte aligned, every aligned run of four cells (a quad) and its +-y
+    // and +-z rows load as float4, so the cell loops issue one load per four
+    // cells per vector instead of one per cell.  The listing then holds the
+    // quads with a liquid cell (QCAP of them), each with its four cells'
+    // stencil words; otherwise the liquid cells one by one (CELL_CAP).
+    //
+    // A block whose cells qualify for the resident operands (one pass, at
+    // most 2 * CG_THREADS liquid cells: chunk_flag counts them, saturated at
+    // 255, so 256 bounds a full chunk) lists cells: with every operand in
+    // shared memory the cell form was faster (CG stage at 128^3 1.69 vs
+    // 1.75 ms per substep); larger blocks take quads (256^3 8.01 vs 8.72 ms).
+    uint32_t liq_bound = 0;
+    if (warp == 0 && m <= KT) {
+        for (uint32_t j = lane; j < m; j += 32) {
+            const uint32_t f = b.chunk_flag[sh.chunk[j]];
+            liq_bound += f == 255u ? 256u : f;
+        }
+        liq_bound = __reduce_add_sync(0xffffffffu, liq_bound);
+        if (lane == 0) sh.u_lb = liq_bound;
+    }
+    __syncthreads();
+    const bool res_fit = m <= KT && sh.u_lb <= 2u * CG_THREADS && A <= RES_MAX_A;
+    __syncthreads();
+    const bool quads = !res_fit && (nx & 3u) == 0u &&
+                       (((uintptr_t)p | (uintptr_t)r | (uintptr_t)q | (uintptr_t)b.dA | (uintptr_t)b.dB) & 15u) == 0u &&
+                       ((uintptr_t)cinfo & 7u) == 0u;
+    uint2* const qlist = reinterpret_cast<uint2*>(sh.cell);
     uint32_t ncell = 0, mc = 0;
-    {
+    if (quads) {
+        // 16 chunks (64 quads each) per round, in (chunk, quad) order; entry
+        // x = stencil words of cells 0..2 (10 bits each), y = cell 3's word |
+        // quad << 10 | chunk slot << 16.
+        const uint32_t lt_mask = (1u << lane) - 1u;
+        for (uint32_t j0 = 0; j0 < mch; j0 += 16) {
+            if ((j0 % KT) == 0 && tid == 0) sh.pass_off[j0 / KT] = ncell;
+            const uint32_t j = j0 + (tid >> 6), qd = tid & 63u;
+            uint2 info = make_uint2(0u, 0u);
+            if (j < mch) {
+                const uint32_t c0 = sh.chunk[j] * CHUNK + 4u * qd;
+                if (c0 < C) info = *reinterpret_cast<const uint2*>(cinfo + c0);  // C is a multiple of 4
+            }
+            const uint32_t w0 = info.x & 1023u, w1 = (info.x >> 16) & 1023u, w2 = info.y & 1023u,
+                           w3 = (info.y >> 16) & 1023u;
+            const bool liq = ((w0 | w1 | w2 | w3) & 1u) != 0u;
+            const uint32_t bal = __ballot_sync(0xffffffffu, liq);
+            if (lane == 0) sh.wcnt[warp] = (uint32_t)__popc(bal);
+            __syncthreads();
+            uint32_t before = 0, total = 0;
+            for (uint32_t w = 0; w < (uint32_t)CG_WARPS; w++) {
+                const uint32_t n = sh.wcnt[w];
+                if (w < warp) before += n;
+                total += n;
+            }
+            __syncthreads();
+            if (ncell + total > QCAP) break;  // uniform: every thread sees the same totals
+            if (liq) qlist[ncell + before + __popc(bal & lt_mask)] = make_uint2(w0 | (w1 << 10) | (w2 << 20), w3 | (qd << 10) | (j << 16));
+            ncell += total;
+            mc = j0 + 16 < mch ? j0 + 16 : mch;
+        }
+    } else {
+        // List the liquid cells of chunks [0, mc), four chunks per round, in
+        // (chunk, cell) order; stop before CELL_CAP would be exceeded.
         const uint32_t lt_mask = (1u << lane) - 1u;
         for (uint32_t j0 = 0; j0 < mch; j0 += 4) {
             if ((j0 % KT) == 0 && tid == 0) sh.pass_off[j0 / KT] = ncell;
@@ -490,7 +563,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // written there, and p is written once at the end; d (phase 1) and r
     // (phase 2) are still stored for the neighbours in other blocks.  At 128^3
     // this took the update phase from 2300 to 1640 cycles per iteration.
-    const bool res = !multi && ncell <= 2u * CG_THREADS && A <= RES_MAX_A;
+    const bool res = !quads && !multi && ncell <= 2u * CG_THREADS && A <= RES_MAX_A;
     float4* const rv4 = reinterpret_cast<float4*>(sh.vals + VALS_HALF);
     if (tid == 0) {
         sh.u_s0 = s0;
@@ -499,6 +572,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         sh.u_npc = npc;
         sh.u_ncell = ncell;
         sh.u_res = res ? 1u : 0u;
+        sh.u_quad = quads ? 1u : 0u;
     }
     if (res)
         for (uint32_t tu = tid; tu < ncell; tu += CG_THREADS) {
@@ -548,29 +622,33 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
         bool ok = true;
         const uint32_t A = sh.off[CHUNK];
         if (x && sh.layout == 0u) {
-            float* buf = sh.vals + warp * 128u;  // per-warp staging of 128 partials
+            float* buf = sh.vals + warp * 256u;  // per-warp staging of 256 partials
             for (uint32_t li = blockIdx.x + warp * G; li < (uint32_t)CHUNK; li += CG_WARPS * G) {
                 const uint32_t lo = sh.off[li], hi = sh.off[li + 1];
                 float s = 0.0f;
-                for (uint32_t e0 = lo; e0 < hi; e0 += 128u) {
+                for (uint32_t e0 = lo; e0 < hi; e0 += 256u) {
+                    // all eight polls of a lane in flight, then the waits (the
+                    // wait after each load serialised them: one round trip per word)
+                    unsigned long long w[8];
 #pragma unroll
-                    for (int k2 = 0; k2 < 4; k2++) {
+                    for (int k2 = 0; k2 < 8; k2++) {
                         const uint32_t e = e0 + lane + 32u * k2;
-                        unsigned long long w = 0ull;
-                        if (e < hi) {
-                            w = ld_tag(x + e, acq);
-                            if ((uint32_t)(w >> 32) != tag && ok) {
-                                w = wait_tag(x + e, tag, st, acq, b.prm);
-                                ok = (uint32_t)(w >> 32) == tag;
-                            }
+                        w[k2] = e < hi ? ld_tag(x + e, acq) : 0ull;
+                    }
+#pragma unroll
+                    for (int k2 = 0; k2 < 8; k2++) {
+                        const uint32_t e = e0 + lane + 32u * k2;
+                        if (e < hi && (uint32_t)(w[k2] >> 32) != tag && ok) {
+                            w[k2] = wait_tag(x + e, tag, st, acq, b.prm);
+                            ok = (uint32_t)(w[k2] >> 32) == tag;
                         }
-                        buf[lane + 32u * k2] = __uint_as_float((uint32_t)w);
+                        buf[lane + 32u * k2] = e < hi ? __uint_as_float((uint32_t)w[k2]) : 0.0f;
                     }
                     __syncwarp();
                     if (lane == 0) {  // cg_reduce_final.wgsl:29-36: in plan order, from +0
                         // entries past the segment's end were staged as +0,
                         // which leaves s (never -0) unchanged
-                        const uint32_t n = hi - e0 < 128u ? hi - e0 : 128u;
+                        const uint32_t n = hi - e0 < 256u ? hi - e0 : 256u;
                         for (uint32_t j = 0; j < n; j += 16) {
                             float t16[16];
 #pragma unroll
@@ -900,6 +978,57 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                     __syncthreads();
                 }
                 const uint32_t beg = sh.pass_off[ps], end = sh.pass_off[ps + 1];
+                if (vld(sh.u_quad)) {
+                    for (uint32_t t = beg + tid; t < end; t += CG_THREADS) {
+                        // One quad: cells c0..c0+3 of one row.  Its own d, r and
+                        // its +-y, +-z rows as float4, the two x edges as scalars;
+                        // the -x/+x neighbours inside the quad are its own cells.
+                        const uint2 e = qlist[t];
+                        const uint32_t w[4] = {e.x & 1023u, (e.x >> 10) & 1023u, (e.x >> 20) & 1023u, e.y & 1023u};
+                        const uint32_t jq = e.y >> 16, qd = (e.y >> 10) & 63u;
+                        const uint32_t c0 = sh.chunk[jq] * CHUNK + 4u * qd;
+                        const uint32_t any = w[0] | w[1] | w[2] | w[3];
+                        const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                        const float4 dc4 = ld_f4(d_src + c0);
+                        const float4 rc4 = first ? z4 : ld_f4(r + c0);
+                        const bool xm = (w[0] & 2u) != 0u, xp = (w[3] & 4u) != 0u;
+                        const float dxm = xm ? d_src[c0 - 1] : 0.0f, rxm = (xm && !first) ? r[c0 - 1] : 0.0f;
+                        const float dxp = xp ? d_src[c0 + 4] : 0.0f, rxp = (xp && !first) ? r[c0 + 4] : 0.0f;
+                        float4 dn4[4], rn4[4];  // -y, +y, -z, +z rows
+                        const uint32_t off4[4] = {c0 - nx, c0 + nx, c0 - nxy, c0 + nxy};
+#pragma unroll
+                        for (int s = 0; s < 4; s++) {
+                            const bool need = (any >> (3 + s)) & 1u;
+                            dn4[s] = need ? ld_f4(d_src + off4[s]) : z4;
+                            rn4[s] = (need && !first) ? ld_f4(r + off4[s]) : z4;
+                        }
+                        // cg_dir.wgsl:30 for the quad, the edges and the rows,
+                        // then cg_spmv.wgsl:46-68 per cell (order -x,+x,-y,+y,-z,+z)
+                        auto dir = [&](float dv, float rv) { return first ? dv : __fadd_rn(rv, __fmul_rn(beta, dv)); };
+                        const float dq[4] = {dir(dc4.x, rc4.x), dir(dc4.y, rc4.y), dir(dc4.z, rc4.z), dir(dc4.w, rc4.w)};
+                        const float dm = dir(dxm, rxm), dp = dir(dxp, rxp);
+                        float ov[4], oq[4], op[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const uint32_t wk = w[k];
+                            float sum = 0.0f;
+                            if (wk & 2u) sum = __fadd_rn(sum, k == 0 ? dm : dq[k > 0 ? k - 1 : 0]);
+                            if (wk & 4u) sum = __fadd_rn(sum, k == 3 ? dp : dq[k < 3 ? k + 1 : 3]);
+#pragma unroll
+                            for (int s = 0; s < 4; s++)
+                                if ((wk >> (3 + s)) & 1u) sum = __fadd_rn(sum, dir(f4_at(dn4[s], k), f4_at(rn4[s], k)));
+                            const bool liq = (wk & 1u) != 0u;
+                            const float qc = __fsub_rn(__fmul_rn((float)((wk >> 7) & 7u), dq[k]), sum);
+                            ov[k] = liq ? dq[k] : 0.0f;
+                            oq[k] = liq ? qc : 0.0f;
+                            op[k] = liq ? __fmul_rn(dq[k], qc) : 0.0f;
+                            if (f64 && liq) acc_add(acc, dq[k], qc);
+                        }
+                        if (!first) st_f4(d_cur + c0, make_float4(ov[0], ov[1], ov[2], ov[3]));
+                        st_f4(q + c0, make_float4(oq[0], oq[1], oq[2], oq[3]));
+                        if (!f64) *reinterpret_cast<float4*>(&sh.tree[jq - j0][4u * qd]) = make_float4(op[0], op[1], op[2], op[3]);
+                    }
+                } else
                 for (uint32_t t = beg + tid; t < end; t += 2 * CG_THREADS) {
                     // two cells in flight: all loads first
                     uint32_t ent[2], cc[2];
@@ -1021,6 +1150,34 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                     __syncthreads();
                 }
                 const uint32_t beg = sh.pass_off[ps], end = sh.pass_off[ps + 1];
+                if (vld(sh.u_quad)) {
+                    for (uint32_t t = beg + tid; t < end; t += CG_THREADS) {
+                        // cg_update.wgsl:33-34 for the quad's liquid cells; the
+                        // others keep their p and r (written back unchanged)
+                        const uint2 e = qlist[t];
+                        const uint32_t w[4] = {e.x & 1u, (e.x >> 10) & 1u, (e.x >> 20) & 1u, e.y & 1u};
+                        const uint32_t jq = e.y >> 16, qd = (e.y >> 10) & 63u;
+                        const uint32_t c0 = sh.chunk[jq] * CHUNK + 4u * qd;
+                        float4 p4 = ld_f4(p + c0), r4 = ld_f4(r + c0);
+                        const float4 d4 = ld_f4(d_cur + c0), q4 = ld_f4(q + c0);
+                        float op[4];
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {
+                            const float pn = __fadd_rn(f4_at(p4, k), __fmul_rn(alpha, f4_at(d4, k)));
+                            const float rc = __fsub_rn(f4_at(r4, k), __fmul_rn(alpha, f4_at(q4, k)));
+                            const bool liq = w[k] != 0u;
+                            if (liq) {
+                                f4_set(p4, k, pn);
+                                f4_set(r4, k, rc);
+                            }
+                            op[k] = liq ? __fmul_rn(rc, rc) : 0.0f;
+                            if (f64 && liq) acc_add(acc, rc, rc);
+                        }
+                        st_f4(p + c0, p4);
+                        st_f4(r + c0, r4);
+                        if (!f64) *reinterpret_cast<float4*>(&sh.tree[jq - j0][4u * qd]) = make_float4(op[0], op[1], op[2], op[3]);
+                    }
+                } else
                 for (uint32_t t = beg + tid; t < end; t += 2 * CG_THREADS) {
                     uint32_t ent[2], cc[2];
                     float pv[2], dv[2], rv[2], qv[2];

@@ -842,7 +842,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
     // stores overlaps the trees (1-2 % of the CG stage at 128^3 against a
     // release store after the trees).
     static_assert(2 * CG_WARPS == KT, "sh.red stages one pass of chunk trees");
-    auto publish_trees = [&](uint32_t j0, uint32_t nb, unsigned long long* slots, uint32_t tag, bool rel) {
+    // With `zero` (passes that share the tree rows), the tree warps clear
+    // the rows they read, so the next pass starts on zeroed rows without a
+    // clearing loop and barrier of its own; the next pass's first barrier
+    // orders this pass's publication before its trees rewrite sh.red.
+    auto publish_trees = [&](uint32_t j0, uint32_t nb, unsigned long long* slots, uint32_t tag, bool rel, bool zero) {
         __syncthreads();
         if (rel && warp == 0) {
             asm volatile("fence.acq_rel.gpu;" ::: "memory");
@@ -851,6 +855,12 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
             for (uint32_t j = w0; j < nb; j += nw) {
                 const float v = chunk_tree(sh.tree[j], lane);
                 if (lane == 0) sh.red[j] = v;
+                if (zero) {
+                    __syncwarp();
+                    float4* row = reinterpret_cast<float4*>(sh.tree[j]);
+                    row[lane] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                    row[lane + 32] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                }
             }
         }
         __syncthreads();
@@ -968,15 +978,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 if (f64) acc_add(acc, dc, qc);
                 else sh.tree[info >> 18][(info >> 10) & 255u] = __fmul_rn(dc, qc);
             }
-            if (!f64) publish_trees(0, vld(sh.u_mc), slotA, tag, false);
+            if (!f64) publish_trees(0, vld(sh.u_mc), slotA, tag, false, false);
         } else {
             uint32_t j0 = 0;
             for (uint32_t ps = 0; ps < vld(sh.u_npc); ps++, j0 += KT) {
                 const uint32_t nb = vld(sh.u_mc) - j0 < KT ? vld(sh.u_mc) - j0 : KT;
-                if (multi && !f64) {
-                    for (uint32_t i = tid; i < nb * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
-                    __syncthreads();
-                }
                 const uint32_t beg = sh.pass_off[ps], end = sh.pass_off[ps + 1];
                 if (vld(sh.u_quad)) {
                     for (uint32_t t = beg + tid; t < end; t += CG_THREADS) {
@@ -1072,10 +1078,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         else sh.tree[(info >> 18) - j0][(info >> 10) & 255u] = __fmul_rn(dc, qc);
                     }
                 }
-                if (!f64) {
-                    publish_trees(j0, nb, slotA, tag, false);
-                    if (ps + 1 < vld(sh.u_npc) || vld(sh.u_mc) < vld(sh.u_m)) __syncthreads();
-                }
+                if (!f64) publish_trees(j0, nb, slotA, tag, false, multi);
             }
             for (j0 = vld(sh.u_mc); j0 < vld(sh.u_m); j0 += KT) {  // chunks beyond the list: one cell slot per thread
                 const uint32_t nb = vld(sh.u_m) - j0 < KT ? vld(sh.u_m) - j0 : KT;
@@ -1106,7 +1109,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                     if (!f64) sh.tree[t / CHUNK][cl] = prod;
                 }
                 if (!f64) {
-                    publish_trees(j0, nb, slotA, tag, false);
+                    publish_trees(j0, nb, slotA, tag, false, true);  // clears its rows for the next phase's passes
                     __syncthreads();
                 }
             }
@@ -1140,15 +1143,11 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                 if (f64) acc_add(acc, rc, rc);
                 else sh.tree[e >> 18][(e >> 10) & 255u] = __fmul_rn(rc, rc);
             }
-            if (!f64) publish_trees(0, vld(sh.u_mc), slotB, tag, true);
+            if (!f64) publish_trees(0, vld(sh.u_mc), slotB, tag, true, false);
         } else {
             uint32_t j0 = 0;
             for (uint32_t ps = 0; ps < vld(sh.u_npc); ps++, j0 += KT) {
                 const uint32_t nb = vld(sh.u_mc) - j0 < KT ? vld(sh.u_mc) - j0 : KT;
-                if (multi && !f64) {
-                    for (uint32_t i = tid; i < nb * CHUNK; i += CG_THREADS) (&sh.tree[0][0])[i] = 0.0f;
-                    __syncthreads();
-                }
                 const uint32_t beg = sh.pass_off[ps], end = sh.pass_off[ps + 1];
                 if (vld(sh.u_quad)) {
                     for (uint32_t t = beg + tid; t < end; t += CG_THREADS) {
@@ -1203,10 +1202,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                         else sh.tree[(ent[u] >> 18) - j0][(ent[u] >> 10) & 255u] = __fmul_rn(rc, rc);
                     }
                 }
-                if (!f64) {
-                    publish_trees(j0, nb, slotB, tag, true);
-                    if (ps + 1 < vld(sh.u_npc) || vld(sh.u_mc) < vld(sh.u_m)) __syncthreads();
-                }
+                if (!f64) publish_trees(j0, nb, slotB, tag, true, multi);
             }
             for (j0 = vld(sh.u_mc); j0 < vld(sh.u_m); j0 += KT) {
                 const uint32_t nb = vld(sh.u_m) - j0 < KT ? vld(sh.u_m) - j0 : KT;
@@ -1226,7 +1222,7 @@ __global__ void __launch_bounds__(CG_THREADS, 1) k_cg(DevBufs b) {
                     if (!f64) sh.tree[t / CHUNK][cl] = prod;
                 }
                 if (!f64) {
-                    publish_trees(j0, nb, slotB, tag, true);
+                    publish_trees(j0, nb, slotB, tag, true, true);  // clears its rows for the next phase's passes
                     __syncthreads();
                 }
             }

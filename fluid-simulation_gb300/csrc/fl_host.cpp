@@ -658,6 +658,42 @@ fl_status fl_get_stage_times(fl_handle* h, double* ms_out, uint64_t* substeps_ou
     return FL_OK;
 }
 
+namespace {
+// gpu/timing.rs:32-59 (FINE_SECTIONS) and :93 (CG_CATS), with the stage that times each.
+struct SectionRow {
+    const char* name;
+    int stage;
+};
+constexpr SectionRow kSections[FL_SECTION_COUNT] = {
+    {"clear", FL_STAGE_SCATTER},       {"mark", FL_STAGE_SORT},          {"sort", FL_STAGE_SORT},
+    {"classify", FL_STAGE_CLASSIFY},   {"scatter", FL_STAGE_SCATTER},    {"normalize_u", FL_STAGE_PREP},
+    {"normalize_v", FL_STAGE_PREP},    {"normalize_w", FL_STAGE_PREP},   {"savevel_u", FL_STAGE_PREP},
+    {"savevel_v", FL_STAGE_PREP},      {"savevel_w", FL_STAGE_PREP},     {"forces_u", FL_STAGE_PREP},
+    {"forces_v", FL_STAGE_PREP},       {"forces_w", FL_STAGE_PREP},      {"bound_pre_u", FL_STAGE_PREP},
+    {"bound_pre_v", FL_STAGE_PREP},    {"bound_pre_w", FL_STAGE_PREP},   {"divergence", FL_STAGE_PREP},
+    {"cg_init", FL_STAGE_PREP},        {"gradient_u", FL_STAGE_GRADIENT}, {"gradient_v", FL_STAGE_GRADIENT},
+    {"gradient_w", FL_STAGE_GRADIENT}, {"bound_post_u", FL_STAGE_GRADIENT}, {"bound_post_v", FL_STAGE_GRADIENT},
+    {"bound_post_w", FL_STAGE_GRADIENT}, {"g2p", FL_STAGE_G2P},         {"cg_spmv", FL_STAGE_CG},
+    {"cg_reduce", FL_STAGE_CG},        {"cg_update", FL_STAGE_CG},       {"cg_scalars", FL_STAGE_CG},
+};
+}  // namespace
+
+const char* fl_section_name(uint32_t i) { return i < FL_SECTION_COUNT ? kSections[i].name : nullptr; }
+
+int fl_section_stage(uint32_t i) { return i < FL_SECTION_COUNT ? kSections[i].stage : -1; }
+
+fl_status fl_get_coarse_times(fl_handle* h, double* ms_out, uint64_t* substeps_out) {
+    if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
+    if (ms_out) {
+        const double* t = h->stage_ms;
+        ms_out[0] = t[FL_STAGE_SORT] + t[FL_STAGE_CLASSIFY] + t[FL_STAGE_SCATTER] + t[FL_STAGE_PREP];
+        ms_out[1] = t[FL_STAGE_CG];
+        ms_out[2] = t[FL_STAGE_GRADIENT] + t[FL_STAGE_G2P];
+    }
+    if (substeps_out) *substeps_out = h->stage_steps;
+    return FL_OK;
+}
+
 fl_status fl_reset_stage_times(fl_handle* h) {
     if (!h) return set_err(nullptr, FL_INVALID_ARG, "handle is NULL");
     for (int k = 0; k < FL_STAGE_COUNT; k++) h->stage_ms[k] = 0.0;

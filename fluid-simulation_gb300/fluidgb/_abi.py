@@ -110,6 +110,10 @@ SIGNATURES = {
     "fl_get_stage_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                           ctypes.POINTER(ctypes.c_uint64)]),
     "fl_reset_stage_times": (ctypes.c_int, [ctypes.c_void_p]),
+    "fl_section_name": (ctypes.c_char_p, [ctypes.c_uint32]),
+    "fl_section_stage": (ctypes.c_int, [ctypes.c_uint32]),
+    "fl_get_coarse_times": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_uint64)]),
     "fl_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "fl_apply_impulse": (ctypes.c_int, [ctypes.c_void_p, _fp]),
     "fl_reset": (ctypes.c_int, [ctypes.c_void_p]),
@@ -173,6 +177,20 @@ SIGNATURES = {
 
 # FL_STAGE_* order (include/fluidgb.h)
 STAGES = ("sort", "classify", "scatter", "prep", "cg", "gradient", "g2p")
+
+
+def section_table(lib=None):
+    """[(reference section name, stage that times it)] for the reference's
+    detailed sections and CG categories (fl_section_name / fl_section_stage)."""
+    lib = lib or load_library()
+    out = []
+    i = 0
+    while True:
+        name = lib.fl_section_name(i)
+        if name is None:
+            return out
+        out.append((name.decode(), STAGES[lib.fl_section_stage(i)]))
+        i += 1
 
 _lib = None
 
@@ -312,6 +330,14 @@ class Fluid:
 
     def reset_stage_times(self):
         self._c(self.lib.fl_reset_stage_times(self.h))
+
+    def coarse_times(self):
+        """({'prep', 'pressure', 'finish': ms total}, substeps timed): the
+        reference's coarse rollup of the stage totals (fl_get_coarse_times)."""
+        ms = (ctypes.c_double * 3)()
+        n = ctypes.c_uint64()
+        self._c(self.lib.fl_get_coarse_times(self.h, ms, ctypes.byref(n)))
+        return {"prep": ms[0], "pressure": ms[1], "finish": ms[2]}, n.value
 
     def sync(self):
         self._c(self.lib.fl_sync(self.h))

@@ -288,6 +288,25 @@ fl_status fl_set_profiling(fl_handle* h, int enable);
 fl_status fl_get_stage_times(fl_handle* h, double* ms_out, uint64_t* substeps_out);
 fl_status fl_reset_stage_times(fl_handle* h);
 
+/* The reference's section names, for per-section comparisons: its detailed
+ * sections (FINE_SECTIONS, gpu/timing.rs:32-59: "clear" .. "g2p", indices
+ * 0-25) followed by its CG categories (CG_CATS, timing.rs:93: "cg_spmv",
+ * "cg_reduce", "cg_update", "cg_scalars", indices 26-29).  Fused kernels time
+ * several sections at once here, so each section reports the FL_STAGE_* whose
+ * time contains it (e.g. "mark" and "sort" -> FL_STAGE_SORT; "clear" ->
+ * FL_STAGE_SCATTER, whose tile kernel writes every face once; the four CG
+ * categories -> FL_STAGE_CG, one persistent kernel).  fl_section_name returns
+ * NULL and fl_section_stage -1 past the end. */
+#define FL_SECTION_COUNT 30u
+const char* fl_section_name(uint32_t i);
+int fl_section_stage(uint32_t i);
+/* The reference's coarse rollup (timing.rs PREP_END / FINISH_START): ms_out[0]
+ * prep (clear .. bound_pre_w), ms_out[1] pressure (divergence, cg_init and the
+ * CG), ms_out[2] finish (gradient .. g2p), from the stage totals.  The grid
+ * prep kernel fuses bound_pre with divergence and cg_init, so its whole time
+ * counts as prep here. */
+fl_status fl_get_coarse_times(fl_handle* h, double* ms_out, uint64_t* substeps_out);
+
 /* ---- scene presets and particle seeding ----
  * The reference's scene presets (app/crates/fluid-lab/src/scene/mod.rs) and
  * its initial particle layout (generate_particles, app/crates/fluid-lab/src/

@@ -38,6 +38,34 @@ def test_abi_version(fluidlib):
     assert fluidlib.fl_abi_version() == 1
 
 
+# The reference's detailed GPU timing sections (gpu/timing.rs:32-59, FINE_SECTIONS)
+# and CG categories (timing.rs:93, CG_CATS), in its order.
+REFERENCE_SECTIONS = [
+    "clear", "mark", "sort", "classify", "scatter", "normalize_u", "normalize_v", "normalize_w", "savevel_u",
+    "savevel_v", "savevel_w", "forces_u", "forces_v", "forces_w", "bound_pre_u", "bound_pre_v", "bound_pre_w",
+    "divergence", "cg_init", "gradient_u", "gradient_v", "gradient_w", "bound_post_u", "bound_post_v",
+    "bound_post_w", "g2p", "cg_spmv", "cg_reduce", "cg_update", "cg_scalars",
+]
+
+
+def test_section_names_are_the_reference_sections(fluidlib):
+    from fluidgb import _abi
+    table = _abi.section_table(fluidlib)
+    assert [n for n, _ in table] == REFERENCE_SECTIONS
+    stage = dict(table)
+    # the coarse rollup's boundaries (timing.rs PREP_END / FINISH_START): every
+    # prep section is timed by a stage of the prep rollup, and so on
+    prep_stages = {"sort", "classify", "scatter", "prep"}
+    for n in REFERENCE_SECTIONS[:REFERENCE_SECTIONS.index("divergence")]:
+        assert stage[n] in prep_stages, n
+    for n in REFERENCE_SECTIONS[REFERENCE_SECTIONS.index("gradient_u"):REFERENCE_SECTIONS.index("g2p") + 1]:
+        assert stage[n] in {"gradient", "g2p"}, n
+    for n in ("cg_spmv", "cg_reduce", "cg_update", "cg_scalars"):
+        assert stage[n] == "cg"
+    assert fluidlib.fl_section_name(len(REFERENCE_SECTIONS)) is None
+    assert fluidlib.fl_section_stage(len(REFERENCE_SECTIONS)) == -1
+
+
 def test_params_layout_is_the_reference_uniform():
     # gpu/fluid.rs:25-39: 8 x vec4 = 128 bytes, then the extension block
     offs = {name: getattr(FlParams, name).offset for name, _ in FlParams._fields_}

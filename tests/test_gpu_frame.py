@@ -92,3 +92,30 @@ def test_seeded_particles_match_the_reference_layout(lib, oracle, preset):
     g.reset()
     assert np.array_equal(g.get_particles()[0], x_ref)
     g.close()
+
+
+def test_stage_times_and_the_reference_rollup(lib):
+    """Profiled substeps give every stage a positive time, and the coarse
+    rollup {prep, pressure, finish} (timing.rs PREP_END / FINISH_START)
+    partitions the stage totals; profiling leaves the results unchanged."""
+    p, parts, _ = scenes.workload("dam32")
+    a = Fluid(p, parts.shape[0])
+    b = Fluid(p, parts.shape[0])
+    a.set_particles(parts)
+    b.set_particles(parts)
+    a.set_profiling(True)
+    a.step(3)
+    b.step(3)
+    stages, n = a.stage_times()
+    coarse, n2 = a.coarse_times()
+    assert n == n2 == 3
+    assert all(v > 0.0 for v in stages.values()), stages
+    assert abs(sum(coarse.values()) - sum(stages.values())) <= 1e-9 * sum(stages.values())
+    assert coarse["pressure"] == stages["cg"]
+    xa, ia = a.get_particles()
+    xb, ib = b.get_particles()
+    assert np.array_equal(xa, xb) and np.array_equal(ia, ib)
+    a.reset_stage_times()
+    assert a.coarse_times() == ({"prep": 0.0, "pressure": 0.0, "finish": 0.0}, 0)
+    a.close()
+    b.close()

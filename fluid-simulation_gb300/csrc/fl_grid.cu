@@ -1,10 +1,11 @@
 // fl_grid.cu — cell classification, P2G, grid preparation and projection.
 //
 //   k_classify   classify.wgsl:25-61 (Solid/Liquid/Air, dilation, liquid count)
-//   k_p2g_tile   scatter.wgsl:44-117 in gather form: one block owns a tile of
-//                faces and accumulates the fixed-point terms of every particle
-//                in the tile and a one-cell halo (read from the sorted bins) in
-//                shared memory; each face is written once, no global atomics
+//   k_p2g_own    scatter.wgsl:44-117 over the sorted bins: one block per tile
+//                of cells accumulates the fixed-point terms of the particles
+//                binned in the tile in shared memory, over the faces they
+//                reach, then adds the sums to the cleared face arrays with
+//                integer reductions (exact and order-free); no float atomics
 //   k_p2g_strays the same terms for particles flagged as strays (their
 //                multiply-form cell differs from their bin), by global atomics
 //   k_grid_prep  normalize.wgsl + save_vel.wgsl + forces.wgsl + boundaries.wgsl
@@ -44,59 +45,57 @@ __global__ void __launch_bounds__(256) k_classify(DevBufs b, uint32_t C) {
 // ---------------------------------------------------------------------------
 // P2G
 
-// k_p2g_tile: one 256-thread block per 8^3 tile of cells.  The tile's halo box
-// (one cell around it) is a set of (y, z) rows, each a contiguous range of the
-// sorted bins; the block flattens them into one index space (row prefix sums
-// in shared memory) so every thread keeps P2G_BATCH particle loads in flight.
-struct TileGeom {
-    int x0, y0, z0;     // first cell of the tile
-    int xe, ye, ze;     // one past the last cell of the tile
-    int n[3];           // grid cells per axis
-};
+constexpr int P2G_BATCH = 4;  // particles in flight per thread
 
-// Face range owned along axis b by the tile, for faces of `axis`.
-__device__ __forceinline__ void owned_range(const TileGeom& T, int axis, int b, int& lo, int& hi) {
-    const int s = b == 0 ? T.x0 : (b == 1 ? T.y0 : T.z0);
-    const int e = b == 0 ? T.xe : (b == 1 ? T.ye : T.ze);
-    lo = s;
-    hi = (axis == b && e == T.n[b]) ? e + 1 : e;
-}
+// k_p2g_own: one 256-thread block per 8^3 tile of cells, visiting only the
+// particles binned in the tile (each particle once; a tile that also read its
+// one-cell halo, to own its faces outright, visited about 1.95 per particle
+// at 128^3).  A particle of cell c
+// reaches faces c..c+1 along the face axis and c-1..c+1 along the other two
+// (scatter.wgsl:55-67), so the block accumulates its fixed-point terms over a
+// box of (TILE+1) x (TILE+2) x (TILE+2) faces per axis -- the tile's faces
+// and a one-face rim -- in shared memory, then adds every nonzero sum to the
+// face arrays (cleared before the launch) with integer reductions.  Integer
+// sums are order-free, so num/den equal the reference's atomic scatter
+// exactly, whatever order the blocks add in.
+constexpr int PB_A = TILE + 1;                  // box faces along the face axis
+constexpr int PB_O = TILE + 2;                  // box faces along the other axes
+constexpr int PB_N = PB_A * PB_O * PB_O;        // box faces per axis
+constexpr int P2G_OWN_ROWS = TILE * TILE;       // (y, z) rows of a tile
 
-constexpr int TS_U = (TILE + 1) * TILE * TILE;  // shared slots per axis
-
-__device__ __forceinline__ void p2g_component(const DevParams& P, const TileGeom& T, int axis, const float q[3],
-                                              float vcomp, int32_t* s_num, int32_t* s_den) {
-    float g[3], t[3];
+__device__ __forceinline__ void p2g_box(const DevParams& P, DevStats* st, const int o[3], int axis, const float q[3],
+                                        float vcomp, int32_t* s_num, int32_t* s_den) {
+    float t[3];
     int base[3];
 #pragma unroll
-    for (int b = 0; b < 3; b++) {
-        g[b] = __fadd_rn(q[b], b == axis ? 0.0f : -0.5f);
-        base[b] = floor_to_i32(g[b]);
-        t[b] = __fsub_rn(g[b], (float)base[b]);
+    for (int bb = 0; bb < 3; bb++) {
+        const float g = __fadd_rn(q[bb], bb == axis ? 0.0f : -0.5f);
+        base[bb] = floor_to_i32(g) - (o[bb] - (bb == axis ? 0 : 1));  // box coordinate of the first tap
+        t[bb] = __fsub_rn(g, floorf(g));
     }
-    int lo[3], hi[3];
-#pragma unroll
-    for (int b = 0; b < 3; b++) owned_range(T, axis, b, lo[b], hi[b]);
-    const int sx = TILE + (axis == 0), sy = TILE + (axis == 1);
+    // A particle that is not a stray has floor(q) == its bin cell, so the taps
+    // lie in the box (first tap 0..TILE-1 along the face axis, 0..TILE along
+    // the others); anything else is recorded and skipped, never written.
+    const uint32_t lim[3] = {axis == 0 ? (uint32_t)TILE - 1u : (uint32_t)TILE, axis == 1 ? (uint32_t)TILE - 1u : (uint32_t)TILE,
+                             axis == 2 ? (uint32_t)TILE - 1u : (uint32_t)TILE};
+    if ((uint32_t)base[0] > lim[0] || (uint32_t)base[1] > lim[1] || (uint32_t)base[2] > lim[2]) {
+        atomicCAS(&st->status, 0u, 7u /* FL_INTERNAL */);
+        return;
+    }
+    const int sx = axis == 0 ? PB_A : PB_O, sy = axis == 1 ? PB_A : PB_O;
     const float scale = P.fixed_scale;
 #pragma unroll
     for (int dk = 0; dk < 2; dk++) {
-        const int kk = base[2] + dk;
-        if (kk < lo[2] || kk >= hi[2]) continue;
         const float wz = tent(t[2], dk);
 #pragma unroll
         for (int dj = 0; dj < 2; dj++) {
-            const int jj = base[1] + dj;
-            if (jj < lo[1] || jj >= hi[1]) continue;
             const float wy = tent(t[1], dj);
 #pragma unroll
             for (int di = 0; di < 2; di++) {
-                const int ii = base[0] + di;
-                if (ii < lo[0] || ii >= hi[0]) continue;
                 const float wx = tent(t[0], di);
                 const float w = __fmul_rn(__fmul_rn(wx, wy), wz);
                 if (w <= 0.0f) continue;
-                const int li = (ii - T.x0) + sx * ((jj - T.y0) + sy * (kk - T.z0));
+                const int li = (base[0] + di) + sx * ((base[1] + dj) + sy * (base[2] + dk));
                 atomicAdd(&s_num[li], fixed_round(__fmul_rn(__fmul_rn(w, vcomp), scale)));
                 atomicAdd(&s_den[li], fixed_round(__fmul_rn(w, scale)));
             }
@@ -104,70 +103,53 @@ __device__ __forceinline__ void p2g_component(const DevParams& P, const TileGeom
     }
 }
 
-constexpr int P2G_ROWS = (TILE + 2) * (TILE + 2);  // halo rows (y, z) of a tile
-constexpr int P2G_BATCH = 4;                        // particles in flight per thread
-
-__global__ void __launch_bounds__(256) k_p2g_tile(DevBufs b, int tiles_x, int tiles_y) {
-    __shared__ int32_t s_num[3][TS_U];
-    __shared__ int32_t s_den[3][TS_U];
-    __shared__ uint32_t s_row_beg[P2G_ROWS];      // first sorted particle of each halo row
-    __shared__ uint32_t s_row_off[P2G_ROWS + 1];  // prefix of the row lengths
-    __shared__ uint32_t s_wsum[4];
+__global__ void __launch_bounds__(256) k_p2g_own(DevBufs b, int tiles_x, int tiles_y) {
+    __shared__ int32_t s_num[3][PB_N];
+    __shared__ int32_t s_den[3][PB_N];
+    __shared__ uint32_t s_row_beg[P2G_OWN_ROWS];      // first sorted particle of each row of the tile
+    __shared__ uint32_t s_row_off[P2G_OWN_ROWS + 1];  // prefix of the row lengths
+    __shared__ uint32_t s_wsum[2];
     const DevParams& P = *b.prm;
     const int nx = (int)P.nx, ny = (int)P.ny, nz = (int)P.nz;
-    const int tid = blockIdx.x;
-    const int tx = tid % tiles_x, ty = (tid / tiles_x) % tiles_y, tz = tid / (tiles_x * tiles_y);
-    TileGeom T;
-    T.x0 = tx * TILE; T.y0 = ty * TILE; T.z0 = tz * TILE;
-    T.xe = min(T.x0 + TILE, nx); T.ye = min(T.y0 + TILE, ny); T.ze = min(T.z0 + TILE, nz);
-    T.n[0] = nx; T.n[1] = ny; T.n[2] = nz;
-    for (int i = threadIdx.x; i < 3 * TS_U; i += blockDim.x) {
-        (&s_num[0][0])[i] = 0;
-        (&s_den[0][0])[i] = 0;
-    }
-
-    // Halo of one cell: every non-stray particle whose taps reach an owned face
-    // has its bin in [x0-1, xe] x [y0-1, ye] x [z0-1, ze] (clamped to the grid).
-    // Each (y, z) row of that box is one contiguous range of the sorted bins.
-    const int hx0 = max(T.x0 - 1, 0), hx1 = min(T.xe, nx - 1);
-    const int hy0 = max(T.y0 - 1, 0), hy1 = min(T.ye, ny - 1);
-    const int hz0 = max(T.z0 - 1, 0), hz1 = min(T.ze, nz - 1);
-    const int rows_y = hy1 - hy0 + 1, rows = rows_y * (hz1 - hz0 + 1);
+    const int tile = blockIdx.x;
+    const int x0 = (tile % tiles_x) * TILE, y0 = ((tile / tiles_x) % tiles_y) * TILE, z0 = (tile / (tiles_x * tiles_y)) * TILE;
+    const int xe = min(x0 + TILE, nx), ye = min(y0 + TILE, ny), ze = min(z0 + TILE, nz);
+    const int rows_y = ye - y0, rows = rows_y * (ze - z0);
     uint32_t len = 0;
     if ((int)threadIdx.x < rows) {
-        const int cy = hy0 + (int)threadIdx.x % rows_y, cz = hz0 + (int)threadIdx.x / rows_y;
-        const uint32_t c0 = (uint32_t)hx0 + P.nx * ((uint32_t)cy + P.ny * (uint32_t)cz);
-        const uint32_t c1 = c0 + (uint32_t)(hx1 - hx0);
+        const uint32_t cy = (uint32_t)(y0 + (int)threadIdx.x % rows_y), cz = (uint32_t)(z0 + (int)threadIdx.x / rows_y);
+        const uint32_t c0 = (uint32_t)x0 + P.nx * (cy + P.ny * cz), c1 = c0 + (uint32_t)(xe - x0 - 1);
         const uint32_t pbeg = b.offsets[c0];
         len = b.offsets[c1] + b.counts[c1] - pbeg;
         s_row_beg[threadIdx.x] = pbeg;
     }
-    // exclusive prefix of the row lengths (rows <= 100 < 128: warps 0..3)
+    // exclusive prefix of the row lengths (rows <= 64: warps 0..1)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
         uint32_t x = len;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += y;
         }
-        if (warp < 4 && lane == 31) s_wsum[warp] = x;
+        if (warp < 2 && lane == 31) s_wsum[warp] = x;
         __syncthreads();
-        if ((int)threadIdx.x < rows) {
-            uint32_t base = 0;
-            for (int w = 0; w < warp; w++) base += s_wsum[w];
-            s_row_off[threadIdx.x] = base + x - len;
-        }
-        if (threadIdx.x == 0) s_row_off[rows] = s_wsum[0] + s_wsum[1] + s_wsum[2] + s_wsum[3];
-        __syncthreads();
+        if ((int)threadIdx.x < rows) s_row_off[threadIdx.x] = (warp == 1 ? s_wsum[0] : 0u) + x - len;
+        if (threadIdx.x == 0) s_row_off[rows] = s_wsum[0] + s_wsum[1];
     }
-    const uint32_t total = s_row_off[rows];
+    const uint32_t total = s_wsum[0] + s_wsum[1];
+    if (total == 0) return;  // no particle binned in the tile: nothing to add (the face arrays are cleared)
+    for (int i = threadIdx.x; i < 3 * PB_N; i += blockDim.x) {
+        (&s_num[0][0])[i] = 0;
+        (&s_den[0][0])[i] = 0;
+    }
+    __syncthreads();
     const float inv_h = P.inv_h;
     const float o0 = P.origin[0], o1 = P.origin[1], o2 = P.origin[2];
-    // Flattened particle index f of the tile's halo box.  Within each group of
-    // 256 indices thread t takes (t % 32) * 8 + t / 32, so the lanes of a warp
-    // hold particles of different cells (8 per cell when dense) and their
-    // shared-memory atomics rarely meet on one face.
+    const int orig[3] = {x0, y0, z0};
+    // Within each group of 256 particle indices thread t takes (t % 32) * 8
+    // + t / 32, so the lanes of a warp hold particles of different cells (8
+    // per cell when dense) and their shared-memory atomics rarely meet.
     const uint32_t swz = (threadIdx.x & 31u) * 8u + (threadIdx.x >> 5);
     for (uint32_t g0 = 0; g0 < total; g0 += 256u * P2G_BATCH) {
         float4 pos[P2G_BATCH], vel[P2G_BATCH];
@@ -194,26 +176,26 @@ __global__ void __launch_bounds__(256) k_p2g_tile(DevBufs b, int tiles_x, int ti
             if (!use[k] || pos[k].w != 0.0f) continue;  // stray: handled by k_p2g_strays
             const float q[3] = {__fmul_rn(__fsub_rn(pos[k].x, o0), inv_h), __fmul_rn(__fsub_rn(pos[k].y, o1), inv_h),
                                 __fmul_rn(__fsub_rn(pos[k].z, o2), inv_h)};
-            p2g_component(P, T, 0, q, vel[k].x, s_num[0], s_den[0]);
-            p2g_component(P, T, 1, q, vel[k].y, s_num[1], s_den[1]);
-            p2g_component(P, T, 2, q, vel[k].z, s_num[2], s_den[2]);
+            p2g_box(P, b.st, orig, 0, q, vel[k].x, s_num[0], s_den[0]);
+            p2g_box(P, b.st, orig, 1, q, vel[k].y, s_num[1], s_den[1]);
+            p2g_box(P, b.st, orig, 2, q, vel[k].z, s_num[2], s_den[2]);
         }
     }
     __syncthreads();
 
-    // Write every owned face once.
+    // Add the box to the face arrays: every nonzero sum of a face inside the grid.
     for (int axis = 0; axis < 3; axis++) {
-        const int sx = TILE + (axis == 0), sy = TILE + (axis == 1), sz = TILE + (axis == 2);
-        int lo[3], hi[3];
-        for (int bb = 0; bb < 3; bb++) owned_range(T, axis, bb, lo[bb], hi[bb]);
-        const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
-        for (int li = threadIdx.x; li < sx * sy * sz; li += blockDim.x) {
-            const int lx = li % sx, ly = (li / sx) % sy, lz = li / (sx * sy);
-            const int fi = T.x0 + lx, fj = T.y0 + ly, fk = T.z0 + lz;
-            if (fi >= hi[0] || fj >= hi[1] || fk >= hi[2]) continue;
-            const size_t gidx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
-            b.num[axis][gidx] = s_num[axis][li];
-            b.den[axis][gidx] = s_den[axis][li];
+        const int sx = axis == 0 ? PB_A : PB_O, sy = axis == 1 ? PB_A : PB_O;
+        const int fx0 = x0 - (axis != 0), fy0 = y0 - (axis != 1), fz0 = z0 - (axis != 2);
+        const int dx = (int)face_dim(P, axis, 0), dy = (int)face_dim(P, axis, 1), dz = (int)face_dim(P, axis, 2);
+        for (int li = threadIdx.x; li < PB_N; li += blockDim.x) {
+            const int32_t vn = s_num[axis][li], vd = s_den[axis][li];
+            if ((vn | vd) == 0) continue;
+            const int fi = fx0 + li % sx, fj = fy0 + (li / sx) % sy, fk = fz0 + li / (sx * sy);
+            if (fi < 0 || fj < 0 || fk < 0 || fi >= dx || fj >= dy || fk >= dz) continue;
+            const size_t gidx = (size_t)fi + (size_t)dx * ((size_t)fj + (size_t)dy * fk);
+            if (vn) atomicAdd(&b.num[axis][gidx], vn);
+            if (vd) atomicAdd(&b.den[axis][gidx], vd);
         }
     }
 }
@@ -508,7 +490,14 @@ cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s) {
 
 cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s) {
     const int tx = (int)((nx + TILE - 1) / TILE), ty = (int)((ny + TILE - 1) / TILE), tz = (int)((nz + TILE - 1) / TILE);
-    k_p2g_tile<<<tx * ty * tz, 256, 0, s>>>(b, tx, ty);
+    // scatter.wgsl's accumulators start at zero (the reference's clear pass)
+    for (int a = 0; a < 3; a++) {
+        const size_t faces = (size_t)(nx + (a == 0)) * (ny + (a == 1)) * (nz + (a == 2));
+        cudaError_t e = cudaMemsetAsync(b.num[a], 0, 4 * faces, s);
+        if (e == cudaSuccess) e = cudaMemsetAsync(b.den[a], 0, 4 * faces, s);
+        if (e != cudaSuccess) return e;
+    }
+    k_p2g_own<<<tx * ty * tz, 256, 0, s>>>(b, tx, ty);
     k_p2g_strays<<<L.num_sms, 256, 0, s>>>(b);
     return cudaGetLastError();
 }

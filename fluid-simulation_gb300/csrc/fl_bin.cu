@@ -144,7 +144,36 @@ __global__ void __launch_bounds__(256) k_bin_scatter(DevBufs b) {
     }
 }
 
-// Sort small buckets in registers; queue large ones for k_bin_fix_big.
+// In-bucket sort of small buckets in registers: Batcher's odd-even merge
+// sort networks for 8 and 16 keys (19 and 63 comparators; each puts the
+// smaller key at the lower index), checked for every 0/1 input (the 0-1
+// principle).  Padding keys are 0xffffffff, above every particle index.
+#define BIN_CX(i, j)                                  \
+    {                                                 \
+        const uint32_t lo_ = min(a[i], a[j]);         \
+        const uint32_t hi_ = max(a[i], a[j]);         \
+        a[i] = lo_;                                   \
+        a[j] = hi_;                                   \
+    }
+__device__ __forceinline__ void sort8(uint32_t (&a)[16]) {
+        BIN_CX(0, 1) BIN_CX(2, 3) BIN_CX(0, 2) BIN_CX(1, 3) BIN_CX(1, 2) BIN_CX(4, 5) BIN_CX(6, 7) BIN_CX(4, 6)
+        BIN_CX(5, 7) BIN_CX(5, 6) BIN_CX(0, 4) BIN_CX(2, 6) BIN_CX(2, 4) BIN_CX(1, 5) BIN_CX(3, 7) BIN_CX(3, 5)
+        BIN_CX(1, 2) BIN_CX(3, 4) BIN_CX(5, 6)
+}
+__device__ __forceinline__ void sort16(uint32_t (&a)[16]) {
+        BIN_CX(0, 1) BIN_CX(2, 3) BIN_CX(0, 2) BIN_CX(1, 3) BIN_CX(1, 2) BIN_CX(4, 5) BIN_CX(6, 7) BIN_CX(4, 6)
+        BIN_CX(5, 7) BIN_CX(5, 6) BIN_CX(0, 4) BIN_CX(2, 6) BIN_CX(2, 4) BIN_CX(1, 5) BIN_CX(3, 7) BIN_CX(3, 5)
+        BIN_CX(1, 2) BIN_CX(3, 4) BIN_CX(5, 6) BIN_CX(8, 9) BIN_CX(10, 11) BIN_CX(8, 10) BIN_CX(9, 11) BIN_CX(9, 10)
+        BIN_CX(12, 13) BIN_CX(14, 15) BIN_CX(12, 14) BIN_CX(13, 15) BIN_CX(13, 14) BIN_CX(8, 12) BIN_CX(10, 14) BIN_CX(10, 12)
+        BIN_CX(9, 13) BIN_CX(11, 15) BIN_CX(11, 13) BIN_CX(9, 10) BIN_CX(11, 12) BIN_CX(13, 14) BIN_CX(0, 8) BIN_CX(4, 12)
+        BIN_CX(4, 8) BIN_CX(2, 10) BIN_CX(6, 14) BIN_CX(6, 10) BIN_CX(2, 4) BIN_CX(6, 8) BIN_CX(10, 12) BIN_CX(1, 9)
+        BIN_CX(5, 13) BIN_CX(5, 9) BIN_CX(3, 11) BIN_CX(7, 15) BIN_CX(7, 11) BIN_CX(3, 5) BIN_CX(7, 9) BIN_CX(11, 13)
+        BIN_CX(1, 2) BIN_CX(3, 4) BIN_CX(5, 6) BIN_CX(7, 8) BIN_CX(9, 10) BIN_CX(11, 12) BIN_CX(13, 14)
+}
+#undef BIN_CX
+
+// Sort small buckets (the networks above up to 16 keys, an insertion sort up
+// to 32); queue large ones for k_bin_fix_big.
 __global__ void __launch_bounds__(256) k_bin_fix(DevBufs b, uint32_t C) {
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
@@ -154,6 +183,17 @@ __global__ void __launch_bounds__(256) k_bin_fix(DevBufs b, uint32_t C) {
     if (n > 32) {
         const uint32_t slot = atomicAdd(&b.st->big_buckets, 1u);
         b.big_list[slot] = c;
+        return;
+    }
+    if (n <= 16) {
+        uint32_t k[16];
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i++) k[i] = i < n ? b.perm[off + i] : 0xffffffffu;
+        if (n <= 8) sort8(k);
+        else sort16(k);
+#pragma unroll
+        for (uint32_t i = 0; i < 16; i++)
+            if (i < n) b.perm[off + i] = k[i];
         return;
     }
     uint32_t a[32];

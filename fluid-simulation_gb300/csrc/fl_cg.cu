@@ -324,16 +324,17 @@ __global__ void __launch_bounds__(CHUNK) k_cg_plan(DevBufs b, uint32_t G) {
     hdr[li] = off;
     if (li == CHUNK - 1) hdr[CHUNK] = off + cnt;
     uint32_t pos = off;
-    uint64_t X = wbase + y - wsum;  // weight of all plan entries before `pos`
+    uint64_t XG = (uint64_t)(wbase + y - wsum) * G;  // G x the weight of all plan entries before `pos`
+    // Blocks bb with X*G < bb*W <= X1*G start after the entry spanning
+    // weights [X, X1).  X only grows along this thread's entries, so the
+    // next such block is tracked incrementally from one division.
+    uint64_t bb_next = W ? XG / W + 1 : 0, bbW = bb_next * W;
     for (uint32_t c = li; c < nchunks; c += CHUNK) {
         const uint32_t f = b.chunk_flag[c];
         if (!f) continue;
         b.cg_chunk[pos] = c;
-        const uint64_t X1 = X + f + CHUNK_WEIGHT;
-        // blocks bb with X*G < bb*W <= X1*G start after this entry
-        const uint64_t lo = X * G / W + 1, hi = X1 * G / W;
-        for (uint64_t bb = lo; bb <= hi; bb++) start[bb] = pos + 1;
-        X = X1;
+        XG += (uint64_t)(f + CHUNK_WEIGHT) * G;
+        for (; bbW <= XG; bb_next++, bbW += W) start[bb_next] = pos + 1;
         pos++;
     }
     if (A == 0)

@@ -282,8 +282,9 @@ struct LaunchCfg {
 };
 cudaError_t launch_bin(const DevBufs& b, const LaunchCfg& L, uint32_t C, uint32_t cap, cudaStream_t s);
 cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s);
+// clear: zero the face accumulators first (unless the caller's memset covers them).
 cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz,
-                       cudaStream_t s);
+                       cudaStream_t s, bool clear);
 cudaError_t launch_grid_prep(const DevBufs& b, uint32_t C, cudaStream_t s);
 // precision: FL_CG_F32, FL_CG_F64 or FL_CG_F64_IEEE (the kernel is specialised per precision).
 cudaError_t launch_cg(const DevBufs& b, const LaunchCfg& L, cudaStream_t s, uint32_t precision);

@@ -488,10 +488,11 @@ cudaError_t launch_classify(const DevBufs& b, uint32_t C, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s) {
+cudaError_t launch_p2g(const DevBufs& b, const LaunchCfg& L, uint32_t nx, uint32_t ny, uint32_t nz, cudaStream_t s,
+                       bool clear) {
     const int tx = (int)((nx + TILE - 1) / TILE), ty = (int)((ny + TILE - 1) / TILE), tz = (int)((nz + TILE - 1) / TILE);
     // scatter.wgsl's accumulators start at zero (the reference's clear pass)
-    for (int a = 0; a < 3; a++) {
+    for (int a = 0; clear && a < 3; a++) {
         const size_t faces = (size_t)(nx + (a == 0)) * (ny + (a == 1)) * (nz + (a == 2));
         cudaError_t e = cudaMemsetAsync(b.num[a], 0, 4 * faces, s);
         if (e == cudaSuccess) e = cudaMemsetAsync(b.den[a], 0, 4 * faces, s);

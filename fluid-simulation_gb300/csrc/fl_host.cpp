@@ -35,6 +35,7 @@ struct fl_handle {
     DevBufs b{};
     void* pool = nullptr;
     size_t pool_bytes = 0;
+    size_t clear_bytes = 0;  // counts .. den[2]: cleared at the start of every substep
     float4* partA = nullptr;
     uint32_t* idsA = nullptr;
     DevParams* dprm = nullptr;
@@ -255,14 +256,17 @@ cudaError_t enqueue_step(fl_handle* h, const DevBufs& b, cudaStream_t s, cudaEve
                          const float* p_replay = nullptr) {
     cudaError_t e;
     auto mark = [&](int i) { return ev ? cudaEventRecord(ev[i], s) : cudaSuccess; };
-    if ((e = cudaMemsetAsync(h->dst, 0, fl::DEVSTATS_STEP_BYTES, s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(b.counts, 0, sizeof(uint32_t) * (size_t)h->C, s)) != cudaSuccess) return e;
     if ((e = mark(0)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(h->dst, 0, fl::DEVSTATS_STEP_BYTES, s)) != cudaSuccess) return e;
+    // the histogram and the P2G accumulators (scatter.wgsl's sums start at
+    // zero: the reference's clear pass), one contiguous span of the pool,
+    // timed with the binning stage
+    if ((e = cudaMemsetAsync(b.counts, 0, h->clear_bytes, s)) != cudaSuccess) return e;
     if ((e = fl::launch_bin(b, h->L, h->C, h->cap, s)) != cudaSuccess) return e;
     if ((e = mark(1)) != cudaSuccess) return e;
     if ((e = fl::launch_classify(b, h->C, s)) != cudaSuccess) return e;
     if ((e = mark(2)) != cudaSuccess) return e;
-    if ((e = fl::launch_p2g(b, h->L, h->nx, h->ny, h->nz, s)) != cudaSuccess) return e;
+    if ((e = fl::launch_p2g(b, h->L, h->nx, h->ny, h->nz, s, false)) != cudaSuccess) return e;
     if ((e = mark(3)) != cudaSuccess) return e;
     if ((e = fl::launch_grid_prep(b, h->C, s)) != cudaSuccess) return e;
     if ((e = mark(4)) != cudaSuccess) return e;
@@ -409,13 +413,19 @@ fl_status fl_create(const fl_params* params, uint32_t capacity, fl_handle** out)
     size_t o_idsA = pl.take<uint32_t>(cap), o_idsB = pl.take<uint32_t>(cap);
     size_t o_keys = pl.take<uint32_t>(cap), o_perm = pl.take<uint32_t>(cap);
     size_t o_scr = pl.take<uint32_t>(cap), o_stray = pl.take<uint32_t>(cap);
-    size_t o_counts = pl.take<uint32_t>(C), o_offs = pl.take<uint32_t>(C), o_cur = pl.take<uint32_t>(C);
-    size_t o_spine = pl.take<uint32_t>(nb), o_big = pl.take<uint32_t>(C);
-    size_t o_ct = pl.take<uint8_t>(C), o_flag = pl.take<uint8_t>(h->nchunks), o_cinfo = pl.take<uint16_t>(C);
+    // The per-substep accumulators (the histogram and P2G's fixed-point
+    // sums) are contiguous, so one memset clears them all (enqueue_step).
     size_t o_num[3], o_den[3], o_vel[3], o_sav[3];
+    size_t o_counts = pl.take<uint32_t>(C);
     for (int a = 0; a < 3; a++) {
         o_num[a] = pl.take<int32_t>(h->F3[a]);
         o_den[a] = pl.take<int32_t>(h->F3[a]);
+    }
+    h->clear_bytes = pl.off - o_counts;
+    size_t o_offs = pl.take<uint32_t>(C), o_cur = pl.take<uint32_t>(C);
+    size_t o_spine = pl.take<uint32_t>(nb), o_big = pl.take<uint32_t>(C);
+    size_t o_ct = pl.take<uint8_t>(C), o_flag = pl.take<uint8_t>(h->nchunks), o_cinfo = pl.take<uint16_t>(C);
+    for (int a = 0; a < 3; a++) {
         o_vel[a] = pl.take<float>(h->F3[a]);
         o_sav[a] = pl.take<float>(h->F3[a]);
     }
@@ -665,7 +675,7 @@ struct SectionRow {
     int stage;
 };
 constexpr SectionRow kSections[FL_SECTION_COUNT] = {
-    {"clear", FL_STAGE_SCATTER},       {"mark", FL_STAGE_SORT},          {"sort", FL_STAGE_SORT},
+    {"clear", FL_STAGE_SORT},          {"mark", FL_STAGE_SORT},          {"sort", FL_STAGE_SORT},
     {"classify", FL_STAGE_CLASSIFY},   {"scatter", FL_STAGE_SCATTER},    {"normalize_u", FL_STAGE_PREP},
     {"normalize_v", FL_STAGE_PREP},    {"normalize_w", FL_STAGE_PREP},   {"savevel_u", FL_STAGE_PREP},
     {"savevel_v", FL_STAGE_PREP},      {"savevel_w", FL_STAGE_PREP},     {"forces_u", FL_STAGE_PREP},

@@ -274,7 +274,7 @@ fl_status fl_step_replay(fl_handle* h, const void* pressure_dev, fl_tape* t);
  * kernel).  While profiling is on, fl_step launches stage by stage and waits at
  * the end of every substep; totals accumulate until fl_reset_stage_times. */
 enum {
-    FL_STAGE_SORT = 0,      /* mark + counting sort (histogram, scan, stable scatter, gather) */
+    FL_STAGE_SORT = 0,      /* clear (histogram, P2G accumulators) + mark + counting sort */
     FL_STAGE_CLASSIFY = 1,  /* classify */
     FL_STAGE_SCATTER = 2,   /* P2G */
     FL_STAGE_PREP = 3,      /* normalize, save_vel, forces, bound_pre, divergence, cg_init */
@@ -293,9 +293,9 @@ fl_status fl_reset_stage_times(fl_handle* h);
  * 0-25) followed by its CG categories (CG_CATS, timing.rs:93: "cg_spmv",
  * "cg_reduce", "cg_update", "cg_scalars", indices 26-29).  Fused kernels time
  * several sections at once here, so each section reports the FL_STAGE_* whose
- * time contains it (e.g. "mark" and "sort" -> FL_STAGE_SORT; "clear" ->
- * FL_STAGE_SCATTER, whose tile kernel writes every face once; the four CG
- * categories -> FL_STAGE_CG, one persistent kernel).  fl_section_name returns
+ * time contains it (e.g. "clear", "mark" and "sort" -> FL_STAGE_SORT: one
+ * memset clears the histogram and the P2G accumulators at the start of the
+ * substep; the four CG categories -> FL_STAGE_CG, one persistent kernel).  fl_section_name returns
  * NULL and fl_section_stage -1 past the end. */
 #define FL_SECTION_COUNT 30u
 const char* fl_section_name(uint32_t i);

@@ -251,35 +251,20 @@ __global__ void __launch_bounds__(256) k_p2g_strays(DevBufs b) {
 
 // One face after normalize -> save_vel -> forces -> boundaries.
 // Returns the pre-force (saved) value in *saved.
-__device__ __forceinline__ float face_pre(const DevBufs& b, const DevParams& P, int axis, uint32_t fi,
-                                          uint32_t fj, uint32_t fk, float* saved) {
-    const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
-    const size_t idx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
-    const int32_t dn = b.den[axis][idx];
+// One face after normalize -> save_vel -> forces -> boundaries, from
+// preloaded values: the face's fixed-point sums (dn, nm), its coordinate
+// along the axis (comp, of nax cells) and the types of the cells below (tl)
+// and above (th) it, CELL_SOLID outside the grid.  Returns the face value;
+// *saved gets the pre-force (saved) value.
+__device__ __forceinline__ float face_value(const DevParams& P, int axis, int32_t dn, int32_t nm, uint32_t comp,
+                                            uint32_t nax, uint8_t tl, uint8_t th, float* saved) {
     float v = 0.0f;
-    if (dn > 0) v = __fdiv_rn(__int2float_rn(b.num[axis][idx]), __int2float_rn(dn));  // normalize.wgsl:21-26
-    *saved = v;                                                                          // save_vel.wgsl:18
-    const uint32_t comp = axis == 0 ? fi : (axis == 1 ? fj : fk);
-    const uint32_t nax = axis == 0 ? P.nx : (axis == 1 ? P.ny : P.nz);
-    const size_t hi_c = (size_t)fi + P.nx * ((size_t)fj + (size_t)P.ny * fk);
-    const size_t step = axis == 0 ? 1 : (axis == 1 ? P.nx : (size_t)P.nx * P.ny);
-    const uint8_t tl = comp > 0 ? b.ct[hi_c - step] : CELL_SOLID;
-    const uint8_t th = comp < nax ? b.ct[hi_c] : CELL_SOLID;
+    if (dn > 0) v = __fdiv_rn(__int2float_rn(nm), __int2float_rn(dn));  // normalize.wgsl:21-26
+    *saved = v;                                                          // save_vel.wgsl:18
     const bool wet = (comp > 0 && tl == CELL_LIQUID) || (comp < nax && th == CELL_LIQUID);
-    if (wet) v = __fadd_rn(v, __fmul_rn(P.grav[axis], P.dt));      // forces.wgsl:75-83
+    if (wet) v = __fadd_rn(v, __fmul_rn(P.grav[axis], P.dt));  // forces.wgsl:75-83
     if (comp == 0 || comp == nax || tl == CELL_SOLID || th == CELL_SOLID) v = 0.0f;  // boundaries.wgsl:43-60
     return v;
-}
-
-__device__ __forceinline__ void face_out(const DevBufs& b, const DevParams& P, int axis, uint32_t fi, uint32_t fj,
-                                         uint32_t fk, float* v_out) {
-    float sv;
-    const float v = face_pre(b, P, axis, fi, fj, fk, &sv);
-    const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
-    const size_t idx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
-    b.vel[axis][idx] = v;
-    b.sav[axis][idx] = sv;
-    if (v_out) *v_out = v;
 }
 
 // cg_reduce.wgsl:38-49 tree over a 256-thread block (s has 256 floats).
@@ -340,42 +325,79 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
     float prod = 0.0f;
     Df pdf = {0.0f, 0.0f};
     if (c < C) {
+        // Every load a cell needs is issued before its results are used: the
+        // lower faces' sums and cell types first, then (liquid cells) the
+        // upper faces', the neighbours' types and pressures; all stores come
+        // after.  The arithmetic is face_value's and apply_A's, in their order.
         const uint32_t nx = P.nx, ny = P.ny, nz = P.nz;
         const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-        float ul, vl, wl;
-        face_out(b, P, 0, i, j, k, &ul);
-        face_out(b, P, 1, i, j, k, &vl);
-        face_out(b, P, 2, i, j, k, &wl);
-        if (i == nx - 1) face_out(b, P, 0, nx, j, k, nullptr);
-        if (j == ny - 1) face_out(b, P, 1, i, ny, k, nullptr);
-        if (k == nz - 1) face_out(b, P, 2, i, j, nz, nullptr);
-        liquid = b.ct[c] == CELL_LIQUID;
+        const size_t nxy = (size_t)nx * ny;
+        const size_t i0 = (size_t)i + (size_t)(nx + 1) * ((size_t)j + (size_t)ny * k);  // u face (i, j, k)
+        const size_t i1 = (size_t)i + (size_t)nx * ((size_t)j + (size_t)(ny + 1) * k);  // v face (i, j, k)
+        const size_t i2 = c;                                                            // w face (i, j, k)
+        const int32_t d0 = b.den[0][i0], n0 = b.num[0][i0], d1 = b.den[1][i1], n1 = b.num[1][i1];
+        const int32_t d2 = b.den[2][i2], n2 = b.num[2][i2];
+        const uint8_t tc = b.ct[c];
+        const uint8_t tmx = i > 0 ? b.ct[c - 1] : CELL_SOLID, tmy = j > 0 ? b.ct[c - nx] : CELL_SOLID,
+                      tmz = k > 0 ? b.ct[c - nxy] : CELL_SOLID;
+        // the grid's far faces, written by the last cell of each line
+        const bool eu = i == nx - 1, ev = j == ny - 1, ew = k == nz - 1;
+        const int32_t ed0 = eu ? b.den[0][i0 + 1] : 0, en0 = eu ? b.num[0][i0 + 1] : 0;
+        const int32_t ed1 = ev ? b.den[1][i1 + nx] : 0, en1 = ev ? b.num[1][i1 + nx] : 0;
+        const int32_t ed2 = ew ? b.den[2][i2 + nxy] : 0, en2 = ew ? b.num[2][i2 + nxy] : 0;
+        float su, sv, sw;
+        const float ul = face_value(P, 0, d0, n0, i, nx, tmx, tc, &su);
+        const float vl = face_value(P, 1, d1, n1, j, ny, tmy, tc, &sv);
+        const float wl = face_value(P, 2, d2, n2, k, nz, tmz, tc, &sw);
+        liquid = tc == CELL_LIQUID;
         if (liquid) {
             // divergence.wgsl:36-58 (liquid cells are interior, so i+1 <= nx-1)
-            float sv;
-            const float uh = face_pre(b, P, 0, i + 1, j, k, &sv);
-            const float vh = face_pre(b, P, 1, i, j + 1, k, &sv);
-            const float wh = face_pre(b, P, 2, i, j, k + 1, &sv);
-            float dv = __fmul_rn(__fadd_rn(__fadd_rn(__fsub_rn(uh, ul), __fsub_rn(vh, vl)), __fsub_rn(wh, wl)), P.inv_h);
-            if (P.stiff > 0.0f && P.rest > 0.0f) {
-                const float over = __fdiv_rn(fmaxf(0.0f, __fsub_rn(__uint2float_rn(b.counts[c]), P.rest)), P.rest);
+            const int32_t du = b.den[0][i0 + 1], nu = b.num[0][i0 + 1], dv = b.den[1][i1 + nx], nv = b.num[1][i1 + nx];
+            const int32_t dw = b.den[2][i2 + nxy], nw = b.num[2][i2 + nxy];
+            const uint8_t tpx = b.ct[c + 1], tpy = b.ct[c + nx], tpz = b.ct[c + nxy];
+            const bool drift_on = P.stiff > 0.0f && P.rest > 0.0f;
+            const uint32_t occ = drift_on ? b.counts[c] : 0u;
+            const bool warm = P.warm != 0u;
+            const size_t nb6[6] = {c - 1, c + 1, c - nx, c + nx, c - nxy, c + nxy};
+            float pn[6];
+#pragma unroll
+            for (int s2 = 0; s2 < 6; s2++) pn[s2] = warm ? b.p[nb6[s2]] : 0.0f;
+            const float p_initial = warm ? b.p[c] : 0.0f;
+            float unused;
+            const float uh = face_value(P, 0, du, nu, i + 1, nx, tc, tpx, &unused);
+            const float vh = face_value(P, 1, dv, nv, j + 1, ny, tc, tpy, &unused);
+            const float wh = face_value(P, 2, dw, nw, k + 1, nz, tc, tpz, &unused);
+            float dvg = __fmul_rn(__fadd_rn(__fadd_rn(__fsub_rn(uh, ul), __fsub_rn(vh, vl)), __fsub_rn(wh, wl)), P.inv_h);
+            if (drift_on) {
+                const float over = __fdiv_rn(fmaxf(0.0f, __fsub_rn(__uint2float_rn(occ), P.rest)), P.rest);
                 const float drift = fminf(__fmul_rn(P.stiff, over), P.drift_clamp);
-                dv = __fsub_rn(dv, drift);
+                dvg = __fsub_rn(dvg, drift);
             }
-            if (b.div) b.div[c] = dv;
-            // cg_init.wgsl:66-81
-            const float rhs = __fmul_rn(-P.scale_rhs, dv);
+            // cg_init.wgsl:66-81; (A p)_c of cg_init.wgsl:24-48, order -x,+x,-y,+y,-z,+z
+            const float rhs = __fmul_rn(-P.scale_rhs, dvg);
+            const uint8_t t6[6] = {tmx, tpx, tmy, tpy, tmz, tpz};
             float ap = 0.0f;
-            if (P.warm) {
-                const float p_initial = b.p[c];
-                ap = apply_A(b.ct, b.p, c, nx, (size_t)nx * ny, p_initial);
-            } else {
-                b.p[c] = 0.0f;
+            uint32_t info = 1u, ncnt = 0u;
+            {
+                float cnt = 0.0f, sum = 0.0f;
+#pragma unroll
+                for (int s2 = 0; s2 < 6; s2++) {
+                    const uint8_t t = t6[s2];
+                    if (t != CELL_SOLID) {
+                        cnt = __fadd_rn(cnt, 1.0f);
+                        ncnt++;
+                        if (t == CELL_LIQUID) sum = __fadd_rn(sum, pn[s2]);
+                    }
+                    if (t == CELL_LIQUID) info |= 2u << s2;
+                }
+                if (warm) ap = __fsub_rn(__fmul_rn(cnt, p_initial), sum);
             }
             const float rc = __fsub_rn(rhs, ap);
+            if (b.div) b.div[c] = dvg;
+            if (!warm) b.p[c] = 0.0f;
             b.r[c] = rc;
             b.dA[c] = rc;
-            b.cinfo[c] = stencil_info(b.ct, c, nx, (size_t)nx * ny);
+            b.cinfo[c] = (uint16_t)(info | (ncnt << 7));
             prod = __fmul_rn(rc, rc);
             pdf = df_prod(rc, rc);
         } else {
@@ -384,6 +406,25 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
             b.dA[c] = 0.0f;
             b.cinfo[c] = 0;
             if (b.div) b.div[c] = 0.0f;
+        }
+        b.vel[0][i0] = ul;
+        b.sav[0][i0] = su;
+        b.vel[1][i1] = vl;
+        b.sav[1][i1] = sv;
+        b.vel[2][i2] = wl;
+        b.sav[2][i2] = sw;
+        float se;
+        if (eu) {
+            b.vel[0][i0 + 1] = face_value(P, 0, ed0, en0, nx, nx, tc, CELL_SOLID, &se);
+            b.sav[0][i0 + 1] = se;
+        }
+        if (ev) {
+            b.vel[1][i1 + nx] = face_value(P, 1, ed1, en1, ny, ny, tc, CELL_SOLID, &se);
+            b.sav[1][i1 + nx] = se;
+        }
+        if (ew) {
+            b.vel[2][i2 + nxy] = face_value(P, 2, ed2, en2, nz, nz, tc, CELL_SOLID, &se);
+            b.sav[2][i2 + nxy] = se;
         }
     }
     const int nliq = __syncthreads_count(liquid);

@@ -442,31 +442,41 @@ __global__ void __launch_bounds__(256) k_grid_prep(DevBufs b, uint32_t C) {
     }
 }
 
-__device__ __forceinline__ void face_project(const DevBufs& b, const DevParams& P, int axis, uint32_t fi,
-                                             uint32_t fj, uint32_t fk) {
-    const uint32_t comp = axis == 0 ? fi : (axis == 1 ? fj : fk);
-    const uint32_t nax = axis == 0 ? P.nx : (axis == 1 ? P.ny : P.nz);
-    if (comp == 0 || comp == nax) return;  // gradient.wgsl:45
-    const size_t hi = (size_t)fi + P.nx * ((size_t)fj + (size_t)P.ny * fk);
-    const size_t lo = hi - (axis == 0 ? 1 : (axis == 1 ? P.nx : (size_t)P.nx * P.ny));
-    const uint8_t lt = b.ct[lo], ht = b.ct[hi];
-    if (lt == CELL_SOLID || ht == CELL_SOLID) return;
-    if (lt != CELL_LIQUID && ht != CELL_LIQUID) return;
-    const uint32_t dx = face_dim(P, axis, 0), dy = face_dim(P, axis, 1);
-    const size_t idx = (size_t)fi + dx * ((size_t)fj + (size_t)dy * fk);
-    const float dp = __fsub_rn(b.p[hi], b.p[lo]);
-    b.vel[axis][idx] = __fsub_rn(b.vel[axis][idx], __fmul_rn(P.coeff_grad, dp));
-}
-
+// gradient.wgsl:23-67 on the cell's three lower faces: an interior face
+// with no solid side and a liquid side gets vel -= coeff * (p_hi - p_lo).
+// The cell types, pressures and face values are loaded before any face is
+// written (the kernel is latency-bound, and a face's store would otherwise
+// hold back the next face's loads).
 __global__ void __launch_bounds__(256) k_project(DevBufs b, uint32_t C) {
     const DevParams& P = *b.prm;
     const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= C) return;
     const uint32_t nx = P.nx, ny = P.ny;
     const uint32_t i = c % nx, j = (c / nx) % ny, k = c / (nx * ny);
-    face_project(b, P, 0, i, j, k);
-    face_project(b, P, 1, i, j, k);
-    face_project(b, P, 2, i, j, k);
+    const size_t nxy = (size_t)nx * ny;
+    const size_t lo[3] = {c - 1, c - nx, c - nxy};
+    const size_t idx[3] = {(size_t)i + (size_t)(nx + 1) * ((size_t)j + (size_t)ny * k),
+                           (size_t)i + (size_t)nx * ((size_t)j + (size_t)(ny + 1) * k), (size_t)c};
+    const bool inner[3] = {i > 0, j > 0, k > 0};  // comp == nax never holds for a lower face (comp < n)
+    const uint8_t ht = b.ct[c];
+    uint8_t lt[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) lt[a] = inner[a] ? b.ct[lo[a]] : CELL_SOLID;
+    bool on[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++)  // gradient.wgsl:45-60
+        on[a] = inner[a] && lt[a] != CELL_SOLID && ht != CELL_SOLID && (lt[a] == CELL_LIQUID || ht == CELL_LIQUID);
+    if (!(on[0] || on[1] || on[2])) return;
+    const float ph = b.p[c];
+    float pl[3], v[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        pl[a] = on[a] ? b.p[lo[a]] : 0.0f;
+        v[a] = on[a] ? b.vel[a][idx[a]] : 0.0f;
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+        if (on[a]) b.vel[a][idx[a]] = __fsub_rn(v[a], __fmul_rn(P.coeff_grad, __fsub_rn(ph, pl[a])));
 }
 
 // Stand-alone solve: cg_init.wgsl:50-87 from a given divergence field (the
